@@ -1,0 +1,814 @@
+/*
+ * pgd_oracle.c -- CPU oracle for PGD's edge-centric graphlet decomposition.
+ *
+ * TEST INFRASTRUCTURE ONLY: this restates the reference algorithm
+ * (nkahmed/PGD graphlet_core.cpp / graphlet_core.h) in plain C so that the
+ * GPU product path can be checked against it.  Only tests/, the smoke check
+ * and the CPU-baseline leg of bench.py load it.  The product library never
+ * links it, and nothing here is a fallback for the product.
+ *
+ * Every function names the reference lines it follows.  Parity of this file
+ * with the reference is pinned by tests/test_oracle.py against the reference's
+ * fixtures and against the reference compiled from source (oracle/_ref/).
+ */
+#define _GNU_SOURCE
+#include "pgd_oracle.h"
+
+#include <ctype.h>
+#include <errno.h>
+#include <limits.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+struct po_graph {
+    int64_t n, m;      /* vertices, undirected edges (edges.size()/2) */
+    int64_t *off;      /* n+1 offsets                                 */
+    int32_t *adj;      /* 2m neighbour ids, reference order            */
+    int32_t *deg;      /* n degrees                                    */
+    int max_degree;
+    int64_t *ev, *eu;  /* e_v / e_u (graphlet_core.cpp:929-949)        */
+    int64_t n_e;       /* entries in ev/eu                             */
+    int32_t *kcore;    /* n+1, reference's 1-based layout              */
+    int max_core;
+    int32_t *ord;      /* E_ordered edge ids                           */
+    int64_t n_ord;
+    uint64_t sums[PO_NSUMS];
+    uint64_t totals[PO_NTOTALS];
+    uint64_t *t_e, *k4_e, *c4_e; /* by edge id                         */
+    uint64_t *micro;   /* n_ord x 8, by E_ordered position             */
+};
+
+static void set_err(char *err, const char *msg) {
+    if (err) { strncpy(err, msg, 255); err[255] = 0; }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Growable pair list used by the readers.                                   */
+typedef struct { int32_t *a, *b; int64_t k, cap; } pairs_t;
+
+static int pairs_push(pairs_t *p, int32_t a, int32_t b) {
+    if (p->k == p->cap) {
+        int64_t nc = p->cap ? p->cap * 2 : 1024;
+        int32_t *na = realloc(p->a, nc * sizeof(int32_t));
+        int32_t *nb = realloc(p->b, nc * sizeof(int32_t));
+        if (!na || !nb) { free(na ? na : p->a); free(nb ? nb : p->b); p->a = p->b = NULL; return -1; }
+        p->a = na; p->b = nb; p->cap = nc;
+    }
+    p->a[p->k] = a; p->b[p->k] = b; p->k++;
+    return 0;
+}
+
+/* Build a CSR from undirected pairs in insertion order: pair i appends b to
+ * row a and a to row b, exactly as the reader's map<int,vector<int>> does
+ * (graphlet_core.cpp:410-411, 448-452). */
+static po_graph *graph_from_pairs(int64_t n, const pairs_t *p, char *err) {
+    po_graph *g = calloc(1, sizeof(po_graph));
+    if (!g) { set_err(err, "out of memory"); return NULL; }
+    g->n = n;
+    g->off = calloc((size_t)n + 1, sizeof(int64_t));
+    g->adj = malloc((size_t)(2 * p->k + 1) * sizeof(int32_t));
+    g->deg = calloc((size_t)n + 1, sizeof(int32_t));
+    if (!g->off || !g->adj || !g->deg) { po_free(g); set_err(err, "out of memory"); return NULL; }
+    for (int64_t i = 0; i < p->k; i++) { g->off[p->a[i] + 1]++; g->off[p->b[i] + 1]++; }
+    for (int64_t v = 0; v < n; v++) g->off[v + 1] += g->off[v];
+    int64_t *fill = malloc((size_t)(n + 1) * sizeof(int64_t));
+    if (!fill) { po_free(g); set_err(err, "out of memory"); return NULL; }
+    memcpy(fill, g->off, (size_t)(n + 1) * sizeof(int64_t));
+    for (int64_t i = 0; i < p->k; i++) {
+        g->adj[fill[p->a[i]]++] = p->b[i];
+        g->adj[fill[p->b[i]]++] = p->a[i];
+    }
+    free(fill);
+    g->m = p->k;
+    return g;
+}
+
+/* remove_multiple_edges (graphlet_core.cpp:530-556): per row keep the first
+ * occurrence of each neighbour. */
+static void remove_multiple_edges(po_graph *g) {
+    int64_t n = g->n;
+    uint8_t *seen = calloc((size_t)n + 1, 1);
+    int64_t w = 0, start;
+    for (int64_t v = 0; v < n; v++) {
+        start = w;
+        for (int64_t j = g->off[v]; j < g->off[v + 1]; j++) {
+            int32_t x = g->adj[j];
+            if (!seen[x]) { seen[x] = 1; g->adj[w++] = x; }
+        }
+        for (int64_t j = start; j < w; j++) seen[g->adj[j]] = 0;
+        g->off[v] = start;
+    }
+    g->off[n] = w;
+    g->m = w / 2;
+    free(seen);
+}
+
+/* vertex_degrees (graphlet_core.cpp:877-891). */
+static void vertex_degrees(po_graph *g) {
+    int md = 0;
+    for (int64_t v = 0; v < g->n; v++) {
+        g->deg[v] = (int32_t)(g->off[v + 1] - g->off[v]);
+        if (g->deg[v] > md) md = g->deg[v];
+    }
+    g->max_degree = md;
+    g->m = g->off[g->n] / 2;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Reader helpers: the reference tokenises with std::string::find + atoi and */
+/* with stringstream >> int; both behaviours are restated here.              */
+
+static ssize_t read_line(FILE *f, char **buf, size_t *cap) {
+    ssize_t len = getline(buf, cap, f);
+    if (len > 0 && (*buf)[len - 1] == '\n') (*buf)[--len] = 0;
+    return len;
+}
+
+/* graphlet_core::get_token (graphlet_core.cpp:231-241): the value is only
+ * assigned when a non-empty token exists; otherwise it keeps its old value. */
+static void take_token(const char *line, const char *delim, size_t *prev, int *v) {
+    size_t len = strlen(line), dl = strlen(delim);
+    const char *hit = (*prev <= len && dl) ? strstr(line + *prev, delim) : NULL;
+    if (hit) {
+        size_t pos = (size_t)(hit - line);
+        if (pos > *prev) {
+            char tmp[64];
+            size_t k = pos - *prev;
+            if (k > 63) k = 63;
+            memcpy(tmp, line + *prev, k);
+            tmp[k] = 0;
+            *v = atoi(tmp);
+        }
+        *prev = pos + 1;
+    } else if (*prev < len) {
+        *v = atoi(line + *prev);
+    }
+}
+
+/* std::istream >> int on a line (C++11 library semantics): skips white space,
+ * parses an optional sign and digits; on failure stores 0 and sets the fail
+ * state so later extractions leave their targets untouched. */
+static int stream_int(const char **s, int *v, int *failed) {
+    if (*failed) return 0;
+    const char *p = *s;
+    while (*p && isspace((unsigned char)*p)) p++;
+    /* end of input while skipping white space: the sentry fails and the
+     * target keeps its value */
+    if (!*p) { *failed = 1; *s = p; return 0; }
+    const char *q = p;
+    if (*q == '+' || *q == '-') q++;
+    if (!isdigit((unsigned char)*q)) { *v = 0; *failed = 1; *s = p; return 0; }
+    char *end;
+    long val = strtol(p, &end, 10);
+    if (val > INT_MAX) val = INT_MAX;
+    if (val < INT_MIN) val = INT_MIN;
+    *v = (int)val;
+    *s = end;
+    return 1;
+}
+
+static const char *file_ext(const char *path) {
+    const char *dot = strrchr(path, '.');
+    return dot ? dot + 1 : "";
+}
+
+/* read_edge_list (graphlet_core.cpp:291-457). */
+static po_graph *read_edge_list(const char *path, char *err) {
+    FILE *f = fopen(path, "r");
+    if (!f) { set_err(err, "file not found"); return NULL; }
+    char *line = NULL;
+    size_t cap = 0;
+    ssize_t len;
+    char delim[4] = "";
+    int v = -1, u = -1, fix_start = 1, have = 0;
+    /* comment block at the top (:307-313) */
+    while ((len = read_line(f, &line, &cap)) >= 0) {
+        if (len > 0 && (line[0] == '#' || line[0] == '%')) {
+            if (strstr(line, "MatrixMarket matrix coordinate pattern symmetric")) strcpy(delim, " ");
+            continue;
+        }
+        have = 1;
+        break;
+    }
+    if (!have) { if (line) line[0] = 0; else { line = malloc(1); line[0] = 0; } }
+    /* detect_delim (:196-228) */
+    if (!delim[0]) {
+        if (strchr(line, ',')) strcpy(delim, ",");
+        else if (strchr(line, '\t')) strcpy(delim, "\t");
+        else if (strstr(line, "   ")) strcpy(delim, "   ");
+        else if (strchr(line, ' ')) strcpy(delim, " ");
+    }
+    if (!delim[0]) {
+        const char *ext = file_ext(path);
+        if (!strcmp(ext, "csv")) strcpy(delim, ",");
+        else if (!strcmp(ext, "tab")) strcpy(delim, "\t");
+        else strcpy(delim, " ");
+    }
+    /* first line: stringstream >> v >> u (:333-338) */
+    int64_t maxid = 0;
+    if (line[0]) {
+        const char *s = line;
+        int failed = 0;
+        stream_int(&s, &v, &failed);
+        stream_int(&s, &u, &failed);
+        if (v == 0 || u == 0) fix_start = 0;
+        /* the reference sizes its lookup table from the later lines only;
+         * cover the first line too (identical results where it is defined). */
+    }
+    int first_v = -1, first_u = -1;
+    int have_first_tokens = 0;
+    if (line[0] && line[0] != '%' && line[0] != '#') {
+        size_t prev = 0;
+        int a = v, b = u;
+        take_token(line, delim, &prev, &a);
+        take_token(line, delim, &prev, &b);
+        first_v = a; first_u = b; have_first_tokens = 1;
+    }
+    /* pass 1: start index and largest id (:343-357) */
+    while ((len = read_line(f, &line, &cap)) >= 0) {
+        if (len == 0) continue;
+        if (line[0] == '%' || line[0] == '#') continue;
+        size_t prev = 0;
+        take_token(line, delim, &prev, &v);
+        take_token(line, delim, &prev, &u);
+        if (v == 0 || u == 0) fix_start = 0;
+        if (v > maxid) maxid = v;
+        if (u > maxid) maxid = u;
+        if (v < 0 || u < 0) { fclose(f); free(line); set_err(err, "negative vertex id"); return NULL; }
+    }
+    if (have_first_tokens) {
+        if (first_v > maxid) maxid = first_v;
+        if (first_u > maxid) maxid = first_u;
+    }
+    fclose(f);
+    /* pass 2: relabel by first appearance, drop self loops (:369-442) */
+    f = fopen(path, "r");
+    if (!f) { free(line); set_err(err, "file not found"); return NULL; }
+    int32_t *lookup = malloc((size_t)(maxid + 2) * sizeof(int32_t));
+    if (!lookup) { fclose(f); free(line); set_err(err, "out of memory"); return NULL; }
+    for (int64_t i = 0; i <= maxid + 1; i++) lookup[i] = -1;
+    pairs_t p = {0};
+    int32_t next_id = 0;
+    int bad = 0;
+    while ((len = read_line(f, &line, &cap)) >= 0) {
+        if (len == 0) continue;
+        if (line[0] == '%' || line[0] == '#') continue;
+        size_t prev = 0;
+        take_token(line, delim, &prev, &v);
+        take_token(line, delim, &prev, &u);
+        /* v and u are rewritten in place, as at :424-440, so a later line
+         * with an empty token inherits the relabelled id */
+        if (fix_start) { v--; u--; }
+        if (v == u) continue;
+        if (v < 0 || u < 0 || v > maxid || u > maxid) { bad = 1; break; }
+        if (lookup[v] == -1) lookup[v] = next_id++;
+        v = lookup[v];
+        if (lookup[u] == -1) lookup[u] = next_id++;
+        u = lookup[u];
+        if (pairs_push(&p, v, u)) { bad = 2; break; }
+    }
+    fclose(f);
+    free(line);
+    free(lookup);
+    if (bad) { free(p.a); free(p.b); set_err(err, bad == 1 ? "vertex id out of range" : "out of memory"); return NULL; }
+    po_graph *g = graph_from_pairs(next_id, &p, err);
+    free(p.a); free(p.b);
+    if (!g) return NULL;
+    remove_multiple_edges(g);
+    vertex_degrees(g);
+    return g;
+}
+
+/* read_mtx (graphlet_core.cpp:459-522): ids-1, no relabel, no dedup,
+ * n = 1 + largest id with an edge. */
+static po_graph *read_mtx(const char *path, char *err) {
+    FILE *f = fopen(path, "r");
+    if (!f) { set_err(err, "file not found"); return NULL; }
+    char *line = NULL;
+    size_t cap = 0;
+    ssize_t len;
+    int have = 0;
+    while ((len = read_line(f, &line, &cap)) >= 0) {
+        if (len > 0 && (line[0] == '#' || line[0] == '%')) continue;
+        have = 1;
+        break;
+    }
+    int v = -1, u = -1, fix_start = 1;
+    if (have && line[0]) {
+        const char *s = line;
+        int failed = 0;
+        stream_int(&s, &v, &failed);
+        stream_int(&s, &u, &failed);
+        if (v == 0 || u == 0) fix_start = 0;
+    }
+    pairs_t p = {0};
+    int64_t maxkey = -1;
+    int bad = 0;
+    while (have && fix_start && (len = read_line(f, &line, &cap)) >= 0) {
+        if (len == 0) continue;
+        if (line[0] == '%' || line[0] == '#') continue;
+        const char *s = line;
+        int failed = 0;
+        stream_int(&s, &v, &failed);
+        stream_int(&s, &u, &failed);
+        v--; u--;
+        if (v == u) continue;
+        if (v < 0 || u < 0) { bad = 1; break; }
+        if (pairs_push(&p, v, u)) { bad = 2; break; }
+        if (v > maxkey) maxkey = v;
+        if (u > maxkey) maxkey = u;
+    }
+    fclose(f);
+    free(line);
+    if (bad) { free(p.a); free(p.b); set_err(err, bad == 1 ? "vertex id < 1 in mtx file" : "out of memory"); return NULL; }
+    po_graph *g = graph_from_pairs(maxkey + 1, &p, err);
+    free(p.a); free(p.b);
+    if (!g) return NULL;
+    vertex_degrees(g);
+    return g;
+}
+
+/* A row with a repeated neighbour makes the reference's marking ambiguous;
+ * both the oracle and the product refuse such (undeduplicated mtx) input. */
+static int has_duplicate_neighbours(const po_graph *g) {
+    uint8_t *seen = calloc((size_t)g->n + 1, 1);
+    int dup = 0;
+    for (int64_t v = 0; v < g->n && !dup; v++) {
+        for (int64_t j = g->off[v]; j < g->off[v + 1]; j++) {
+            if (seen[g->adj[j]]) { dup = 1; break; }
+            seen[g->adj[j]] = 1;
+        }
+        for (int64_t j = g->off[v]; j < g->off[v + 1]; j++) seen[g->adj[j]] = 0;
+    }
+    free(seen);
+    return dup;
+}
+
+po_graph *po_read_file(const char *path, char *err) {
+    /* read_graph dispatch (graphlet_core.cpp:259-283) */
+    po_graph *g = !strcmp(file_ext(path), "mtx") ? read_mtx(path, err) : read_edge_list(path, err);
+    if (g && has_duplicate_neighbours(g)) {
+        po_free(g);
+        set_err(err, "duplicate entries in mtx input");
+        return NULL;
+    }
+    return g;
+}
+
+po_graph *po_from_csr(int64_t n, const int64_t *off, const int32_t *adj, char *err) {
+    if (n < 0 || off[0] != 0) { set_err(err, "bad csr"); return NULL; }
+    po_graph *g = calloc(1, sizeof(po_graph));
+    if (!g) { set_err(err, "out of memory"); return NULL; }
+    int64_t nnz = off[n];
+    g->n = n;
+    g->off = malloc((size_t)(n + 1) * sizeof(int64_t));
+    g->adj = malloc((size_t)(nnz + 1) * sizeof(int32_t));
+    g->deg = calloc((size_t)n + 1, sizeof(int32_t));
+    if (!g->off || !g->adj || !g->deg) { po_free(g); set_err(err, "out of memory"); return NULL; }
+    memcpy(g->off, off, (size_t)(n + 1) * sizeof(int64_t));
+    memcpy(g->adj, adj, (size_t)nnz * sizeof(int32_t));
+    for (int64_t i = 0; i < nnz; i++)
+        if (adj[i] < 0 || adj[i] >= n) { po_free(g); set_err(err, "neighbour id out of range"); return NULL; }
+    vertex_degrees(g);
+    if (has_duplicate_neighbours(g)) { po_free(g); set_err(err, "duplicate neighbours"); return NULL; }
+    return g;
+}
+
+po_graph *po_from_pairs(int64_t k, const int32_t *src, const int32_t *dst, int64_t n_min,
+                        int dedup, char *err) {
+    pairs_t p = {0};
+    int64_t maxkey = -1;
+    for (int64_t i = 0; i < k; i++) {
+        int32_t a = src[i], b = dst[i];
+        if (a < 0 || b < 0) { free(p.a); free(p.b); set_err(err, "negative vertex id"); return NULL; }
+        if (a == b) continue;
+        if (pairs_push(&p, a, b)) { set_err(err, "out of memory"); return NULL; }
+        if (a > maxkey) maxkey = a;
+        if (b > maxkey) maxkey = b;
+    }
+    int64_t n = maxkey + 1 > n_min ? maxkey + 1 : n_min;
+    po_graph *g = graph_from_pairs(n, &p, err);
+    free(p.a); free(p.b);
+    if (!g) return NULL;
+    if (dedup) remove_multiple_edges(g);
+    vertex_degrees(g);
+    if (!dedup && has_duplicate_neighbours(g)) { po_free(g); set_err(err, "duplicate edges"); return NULL; }
+    return g;
+}
+
+void po_free(po_graph *g) {
+    if (!g) return;
+    free(g->off); free(g->adj); free(g->deg); free(g->ev); free(g->eu);
+    free(g->kcore); free(g->ord); free(g->t_e); free(g->k4_e); free(g->c4_e); free(g->micro);
+    free(g);
+}
+
+/* ------------------------------------------------------------------------ */
+/* compute_cores (graphlet_core.cpp:958-1018).  Core numbers are unique, so  */
+/* any correct peeling gives them; what is restated exactly is the layout:   */
+/* kcore[x] holds the core number of vertex x-1 (kcore[0] = 0), and the     */
+/* reported maximum skips the last vertex (the final loop at :1012-1015     */
+/* reads kcore[] with 0-based ids).                                          */
+int po_compute_cores(po_graph *g) {
+    if (g->kcore) return 0;
+    int64_t n = g->n;
+    int32_t *d = malloc((size_t)(n + 1) * sizeof(int32_t));
+    int32_t *vert = malloc((size_t)(n + 1) * sizeof(int32_t));
+    int32_t *pos = malloc((size_t)(n + 1) * sizeof(int32_t));
+    int md = g->max_degree;
+    int64_t *bin = calloc((size_t)md + 2, sizeof(int64_t));
+    if (!d || !vert || !pos || !bin) { free(d); free(vert); free(pos); free(bin); return -1; }
+    for (int64_t v = 0; v < n; v++) { d[v] = g->deg[v]; bin[d[v]]++; }
+    int64_t start = 0;
+    for (int k = 0; k <= md; k++) { int64_t c = bin[k]; bin[k] = start; start += c; }
+    for (int64_t v = 0; v < n; v++) { pos[v] = (int32_t)bin[d[v]]; vert[pos[v]] = (int32_t)v; bin[d[v]]++; }
+    for (int k = md; k > 0; k--) bin[k] = bin[k - 1];
+    bin[0] = 0;
+    for (int64_t i = 0; i < n; i++) {
+        int32_t v = vert[i];
+        for (int64_t j = g->off[v]; j < g->off[v + 1]; j++) {
+            int32_t x = g->adj[j];
+            if (d[x] > d[v]) {
+                int dx = d[x];
+                int32_t px = pos[x];
+                int32_t pw = (int32_t)bin[dx];
+                int32_t w = vert[pw];
+                if (x != w) { pos[x] = pw; vert[px] = w; pos[w] = px; vert[pw] = x; }
+                bin[dx]++;
+                d[x]--;
+            }
+        }
+    }
+    g->kcore = calloc((size_t)n + 2, sizeof(int32_t));
+    g->kcore[0] = 0;
+    for (int64_t v = 0; v < n; v++) g->kcore[v + 1] = d[v];
+    int mc = 0;
+    for (int64_t v = 0; v + 1 < n; v++) if (d[v] > mc) mc = d[v];
+    g->max_core = mc;
+    free(d); free(vert); free(pos); free(bin);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Neighbour ordering: bucket_sort_neighbors_parallel (graphlet_core.cpp:    */
+/* 1846-1877) is a stable counting sort by key, reversed for the default     */
+/* descending direction.                                                     */
+typedef struct { int32_t key, pos, val; } kp_t;
+
+static int cmp_kp_stable(const void *a, const void *b) {
+    const kp_t *x = a, *y = b;
+    if (x->key != y->key) return x->key < y->key ? -1 : 1;
+    return x->pos < y->pos ? -1 : (x->pos > y->pos);
+}
+
+static void sort_rows_by(po_graph *g, const int32_t *key, int s2l) {
+    int md = g->max_degree;
+    kp_t *buf = malloc((size_t)(md + 1) * sizeof(kp_t));
+    for (int64_t v = 0; v < g->n; v++) {
+        int64_t b = g->off[v], d = g->off[v + 1] - b;
+        for (int64_t j = 0; j < d; j++) {
+            buf[j].key = key[g->adj[b + j]];
+            buf[j].pos = (int32_t)j;
+            buf[j].val = g->adj[b + j];
+        }
+        qsort(buf, (size_t)d, sizeof(kp_t), cmp_kp_stable);
+        if (s2l) for (int64_t j = 0; j < d; j++) g->adj[b + j] = buf[j].val;
+        else for (int64_t j = 0; j < d; j++) g->adj[b + j] = buf[d - 1 - j].val;
+    }
+    free(buf);
+}
+
+int po_preprocess(po_graph *g, const char *neigh_order, int s2l) {
+    /* order_vertex_neighbors (graphlet_core.cpp:1910-1953): "degree"/"deg"
+     * and "kcore" are the deterministic strategies; any other name leaves the
+     * rows as read.  "rand" is wall-clock seeded and not restated. */
+    if (!strcmp(neigh_order, "degree") || !strcmp(neigh_order, "deg")) {
+        sort_rows_by(g, g->deg, s2l);
+    } else if (!strcmp(neigh_order, "kcore")) {
+        if (po_compute_cores(g)) return -1;
+        sort_rows_by(g, g->kcore, s2l);
+    } else if (!strcmp(neigh_order, "rand") || !strcmp(neigh_order, "degree_kcore") ||
+               !strcmp(neigh_order, "deg_kcore") || !strcmp(neigh_order, "degree_vol") ||
+               !strcmp(neigh_order, "deg_vol") || !strcmp(neigh_order, "kcore_vol") ||
+               !strcmp(neigh_order, "degree_kcore_vol") || !strcmp(neigh_order, "deg_kcore_vol")) {
+        return -2;
+    }
+    /* create_edge_list_arrays (graphlet_core.cpp:929-949) */
+    free(g->ev); free(g->eu);
+    g->ev = malloc((size_t)(g->m + 1) * sizeof(int64_t));
+    g->eu = malloc((size_t)(g->m + 1) * sizeof(int64_t));
+    int64_t k = 0;
+    for (int64_t v = 0; v < g->n; v++) {
+        for (int64_t j = g->off[v]; j < g->off[v + 1]; j++) {
+            int64_t u = g->adj[j];
+            if (v < u) {
+                if (g->deg[v] < g->deg[u]) { g->ev[k] = v; g->eu[k] = u; }
+                else { g->ev[k] = u; g->eu[k] = v; }
+                k++;
+            }
+        }
+    }
+    g->n_e = k;
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* sort_edges (graphlet_core.cpp:854-867) with get_ordering_value (:774-834)*/
+/* and the Vertex comparators (graphlet_vertex.h:39-76): the key is stored   */
+/* as int, ties break on edge id, always descending by id.                   */
+typedef struct { int32_t id, key; } ek_t;
+static int cmp_decr(const void *a, const void *b) {
+    const ek_t *x = a, *y = b;
+    if (x->key != y->key) return x->key > y->key ? -1 : 1;
+    return x->id > y->id ? -1 : (x->id < y->id);
+}
+static int cmp_incr(const void *a, const void *b) {
+    const ek_t *x = a, *y = b;
+    if (x->key != y->key) return x->key < y->key ? -1 : 1;
+    return x->id > y->id ? -1 : (x->id < y->id);
+}
+
+int po_sort_edges(po_graph *g, const char *order, int s2l) {
+    int kind;
+    if (!strcmp(order, "natural")) kind = 0;
+    else if (!strcmp(order, "deg") || !strcmp(order, "degree")) kind = 2;
+    else if (!strcmp(order, "kcore") || !strcmp(order, "kcores")) kind = 3;
+    else if (!strcmp(order, "kcore_deg") || !strcmp(order, "kcore_degree")) kind = 4;
+    else if (!strcmp(order, "deg_vol") || !strcmp(order, "degree_vol")) kind = 5;
+    else if (!strcmp(order, "kcore_vol") || !strcmp(order, "kcore_volume")) kind = 6;
+    else if (!strcmp(order, "kcore_deg_vol") || !strcmp(order, "kcore_degree_vol")) kind = 7;
+    else if (!strcmp(order, "rand") || !strcmp(order, "random") || !strcmp(order, "var")) return -2;
+    else kind = 0;
+    /* names that map to enum values past VAR fall to the default branch:
+     * key = degree of e_u (graphlet_core.cpp:829-832). */
+    static const char *deg_u_names[] = {"triangles", "tri", "triangle", "wedges", "tcores", "triangle_cores",
+        "triangle_core", "tcore", "coloring", "greedy_coloring", "tri_vol", "triangle_vol", "tcore_vol",
+        "tcore_volume", "triangle_core_vol", "triangles_only", "triangle_only", "dynamic_largest_first",
+        "lfo", "LFO", "triangle_core_max", "tcore_max", "tcores_max", "degree_triangles", "degree_tri",
+        "deg_tri", "deg_triangles", "kcore_tri", "kcore_triangles", "kcore_triangle", "kcore_deg_tri",
+        "kcore_degree_triangle", "kcore_degree_tri", "kcore_tri_vol", "kcore_triangle_vol",
+        "kcore_deg_tri_vol", "kcore_degree_tri_vol", "dist_two_lfo", "dist_two_largest_first",
+        "dist_two_dlfo", "dist_two_dynamic_lfo", "dist_two_slo", "dist_two_smallest_last", "ido",
+        "incidence", "incidence_deg", "dist_two_ido", "dist_two_incidence", "dist_two_tcore",
+        "dist_two_triangle_core", "tcore_min", "triangle_core_min", "tri_core_min", "common",
+        "common_neighbors", NULL};
+    for (int i = 0; deg_u_names[i]; i++) if (!strcmp(order, deg_u_names[i])) kind = 99;
+    if (kind == 3 || kind == 4 || kind == 6 || kind == 7) if (po_compute_cores(g)) return -1;
+    int64_t m = g->n_e;
+    ek_t *e = malloc((size_t)(m + 1) * sizeof(ek_t));
+    for (int64_t i = 0; i < m; i++) {
+        int64_t v = g->ev[i], u = g->eu[i];
+        long long val = i;
+        switch (kind) {
+        case 2: val = g->deg[u] + g->deg[v]; break;
+        case 3: val = g->kcore[u] + g->kcore[v]; break;
+        case 4: val = (long long)(g->deg[u] + g->deg[v]) * (g->kcore[u] + g->kcore[v]); break;
+        case 5: case 6: case 7: {
+            val = 0;
+            for (int side = 0; side < 2; side++) {
+                int64_t x = side ? v : u;
+                for (int64_t j = g->off[x]; j < g->off[x + 1]; j++) {
+                    int32_t y = g->adj[j];
+                    long long dy = g->off[y + 1] - g->off[y];
+                    if (kind == 5) val += dy;
+                    else if (kind == 6) val += g->kcore[y];
+                    else val += dy * g->kcore[y];
+                }
+            }
+            break;
+        }
+        case 99: val = g->off[u + 1] - g->off[u]; break;
+        default: break;
+        }
+        e[i].id = (int32_t)i;
+        e[i].key = (int32_t)val;
+    }
+    qsort(e, (size_t)m, sizeof(ek_t), s2l ? cmp_incr : cmp_decr);
+    free(g->ord);
+    g->ord = malloc((size_t)(m + 1) * sizeof(int32_t));
+    for (int64_t i = 0; i < m; i++) g->ord[i] = e[i].id;
+    g->n_ord = m;
+    free(e);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* compute_assortativity (graphlet_core.cpp:1029-1057).  Degree products are */
+/* formed in int as the reference does; the double sums are accumulated in  */
+/* edge order (the reference's OpenMP reduction order is unspecified, so    */
+/* only the printed 6 significant digits are comparable).                    */
+double po_assortativity(po_graph *g) {
+    double mu = 0, jd = 0, psi = 0;
+    for (int64_t e = 0; e < g->n_e; e++) {
+        int dv = g->deg[g->ev[e]], du = g->deg[g->eu[e]];
+        int p = (int)((unsigned)dv * (unsigned)du);
+        int s2 = (int)((unsigned)dv * (unsigned)dv + (unsigned)du * (unsigned)du);
+        mu += (double)p;
+        jd += 0.5 * (double)(dv + du);
+        psi += 0.5 * (double)s2;
+    }
+    double m = (double)g->n_e;
+    double tau = (jd / m) * (jd / m);
+    double r = ((mu / m) - tau) / ((psi / m) - tau);
+    if (r != r) r = 1;
+    if (r < -1 || r > 1.0) r = 1;
+    if (m == 0) r = 0.0;
+    return r;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Per-edge closed forms (solve_graphlet_equations, graphlet_core.cpp:       */
+/* 1326-1364).  Types follow the reference: degrees are long long, t and the */
+/* partial sums unsigned long long; the "/ 2.0" terms take a double round    */
+/* trip and truncate back.                                                   */
+typedef unsigned long long ull;
+
+static inline ull half_d(ull x) { return (ull)((double)x * 0.5); }
+
+static inline void edge_sums(ull *s, long long dv, long long du, ull t, long long m, long long n) {
+    ull star = (ull)dv - t - 1;
+    star = star + (ull)du - t - 1;
+    ull disc = (ull)n - (star + t) - 2;
+    ull sv = (ull)dv - t - 1, su = (ull)du - t - 1;
+    s[0] += t;
+    s[1] += star;
+    s[2] += disc;
+    s[5] += half_d((t + star) * (t + star - 1));  /* N1 */
+    s[6] += half_d(star * (star - 1));            /* N2 */
+    s[7] += half_d(t * (t - 1));                  /* N3 */
+    s[8] += t * star;                             /* N4 */
+    s[9] += sv * su;                              /* N5 */
+    s[10] += (sv * (sv - 1)) / 2 + (su * (su - 1)) / 2; /* N6 */
+    s[11] += (ull)(m - dv - du + 1);              /* N7 */
+    s[12] += half_d(disc * (disc - 1));           /* N8 */
+    s[13] += star * disc;                         /* N9 */
+    s[14] += t * disc;                            /* N10 */
+}
+
+/* Closing identities (graphlet_core.cpp:1449-1472) and compute_4indep
+ * (graphlet_core.h:548-557).  The reference is built with -ffast-math, under
+ * which g++ turns x/3.0 and x/6.0 into multiplications by the rounded
+ * reciprocal; /2.0 and /4.0 are exact either way.  Those are spelled out. */
+void po_close(const uint64_t s[PO_NSUMS], int64_t n_, int64_t m_, uint64_t out[PO_NTOTALS]) {
+    const double third = 1.0 / 3.0, sixth = 1.0 / 6.0;
+    long long n = n_, m = m_;
+    ull N3 = s[7], N4 = s[8], N5 = s[9], N6 = s[10], N7 = s[11], N8 = s[12], N9 = s[13], N10 = s[14];
+    ull t2_1edge = (ull)m;
+    ull t2_indep = (ull)((double)(long long)((ull)n * (ull)(n - 1)) * 0.5 - (double)m);
+    ull t3_tris = (ull)((double)s[0] * third);
+    ull t2_star = (ull)((double)s[1] * 0.5);
+    ull t3_1edge = s[2];
+    long long p3 = (long long)((ull)n * (ull)(n - 1) * (ull)(n - 2));
+    ull t3_indep = (ull)(p3 / 6);
+    t3_indep = t3_indep - (t3_tris + t2_star + t3_1edge);
+    ull clique = (ull)((double)s[3] * sixth);
+    ull chord = N3 - 6 * clique;
+    ull cycle = (ull)((double)s[4] * 0.25);
+    ull path = N5 - 4 * cycle;
+    ull tailed = (ull)((double)(N4 - 4 * chord) * 0.5);
+    ull star3 = (ull)((double)(N6 - tailed) * third);
+    ull e2 = N7;
+    e2 = e2 - 6 * clique - 4 * cycle - 4 * chord - 2 * path - 2 * tailed;
+    e2 = (ull)((double)e2 * 0.5);
+    ull e1 = N8 - 2 * e2;
+    ull st2 = N9 - 2 * path;
+    st2 = (ull)((double)st2 * 0.5);
+    ull tri4 = N10 - tailed;
+    tri4 = (ull)((double)tri4 * third);
+    ull un = (ull)n;
+    ull indep = (un * (un - 1) * (un - 2) * (un - 3)) / 24;
+    indep = indep - (clique + chord + cycle + path + tailed + star3);
+    indep = indep - (e2 + e1 + st2 + tri4);
+    /* field order of graphlet_core.h:310-329 */
+    out[0] = t2_1edge; out[1] = t2_indep;
+    out[2] = t3_tris; out[3] = t2_star; out[4] = t3_1edge; out[5] = t3_indep;
+    out[6] = clique; out[7] = chord; out[8] = tailed; out[9] = cycle; out[10] = star3; out[11] = path;
+    out[12] = e2; out[13] = e1; out[14] = st2; out[15] = tri4; out[16] = indep;
+}
+
+/* ------------------------------------------------------------------------ */
+/* The per-edge loop (graphlet_core.cpp:1408-1424 global, 1549-1577 micro):  */
+/* mark N(v)\{u}, split N(u)\{v} into T (marked) and S_u, count edges from   */
+/* S_u into S_v (induced 4-cycles) and edges inside T (4-cliques).           */
+int po_decompose(po_graph *g, int micro, int threads, int cheap_side) {
+    if (!g->ord) { if (po_sort_edges(g, "deg", 0)) return -1; }
+    int64_t n = g->n, m = g->m, ne = g->n_ord;
+    free(g->t_e); free(g->k4_e); free(g->c4_e); free(g->micro);
+    g->t_e = calloc((size_t)g->n_e + 1, sizeof(ull));
+    g->k4_e = calloc((size_t)g->n_e + 1, sizeof(ull));
+    g->c4_e = calloc((size_t)g->n_e + 1, sizeof(ull));
+    g->micro = micro ? calloc((size_t)(ne + 1) * PO_NMICRO, sizeof(ull)) : NULL;
+    if (!g->t_e || !g->k4_e || !g->c4_e || (micro && !g->micro)) return -1;
+    ull *vol2 = NULL;
+    if (cheap_side) {
+        vol2 = malloc((size_t)(n + 1) * sizeof(ull));
+        for (int64_t x = 0; x < n; x++) {
+            ull s = 0;
+            for (int64_t j = g->off[x]; j < g->off[x + 1]; j++) s += (ull)g->deg[g->adj[j]];
+            vol2[x] = s;
+        }
+    }
+    ull total[PO_NSUMS];
+    memset(total, 0, sizeof(total));
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+#pragma omp parallel
+    {
+        uint8_t *ind = calloc((size_t)n + 1, 1);
+        int32_t *T = malloc((size_t)(g->max_degree + 1) * sizeof(int32_t));
+        int32_t *S = malloc((size_t)(g->max_degree + 1) * sizeof(int32_t));
+        ull loc[PO_NSUMS];
+        memset(loc, 0, sizeof(loc));
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t e = 0; e < ne; e++) {
+            int32_t id = g->ord[e];
+            long long v = g->ev[id], u = g->eu[id];
+            long long dv = g->deg[v], du = g->deg[u];
+            /* mark side a, scan side b; the reference uses a = e_v, b = e_u */
+            long long a = v, b = u;
+            if (cheap_side && vol2[u] > vol2[v]) { a = u; b = v; }
+            for (int64_t j = g->off[a]; j < g->off[a + 1]; j++) if (g->adj[j] != b) ind[g->adj[j]] = 1;
+            ull t = 0, ns = 0;
+            for (int64_t j = g->off[b]; j < g->off[b + 1]; j++) {
+                int32_t w = g->adj[j];
+                if (w == a) continue;
+                if (ind[w] == 1) { ind[w] = 3; T[t++] = w; }
+                else { S[ns++] = w; }
+            }
+            edge_sums(loc, dv, du, t, m, n);
+            ull c4 = 0, k4 = 0;
+            for (ull i = 0; i < ns; i++) {
+                int32_t w = S[i];
+                for (int64_t j = g->off[w]; j < g->off[w + 1]; j++) c4 += (ind[g->adj[j]] == 1);
+            }
+            for (ull i = 0; i < t; i++) {
+                int32_t w = T[i];
+                for (int64_t j = g->off[w]; j < g->off[w + 1]; j++) k4 += (ind[g->adj[j]] == 3);
+                ind[w] = 0;
+            }
+            for (int64_t j = g->off[a]; j < g->off[a + 1]; j++) ind[g->adj[j]] = 0;
+            loc[3] += k4;
+            loc[4] += c4;
+            g->t_e[id] = t; g->k4_e[id] = k4; g->c4_e[id] = c4;
+            if (micro) {
+                /* micro stores (graphlet_core.cpp:1559-1575) and the 2-star
+                 * column of the writer (graphlet_core.h:353-355) */
+                ull *row = (ull *)(g->micro + (size_t)e * PO_NMICRO);
+                long long sv = dv - (long long)t - 1, su = du - (long long)t - 1;
+                ull star3 = (ull)((double)(sv * (sv - 1)) * 0.5);
+                star3 = (ull)((double)star3 + (double)(su * (su - 1)) * 0.5);
+                row[0] = t;
+                row[1] = ((ull)dv - t) + ((ull)du - t) - 2;
+                row[2] = k4;
+                row[3] = (ull)((double)(t * (t - 1)) * 0.5 - (double)k4);
+                row[4] = 0; /* local_4_tailed_tris is never written (:1501) */
+                row[5] = c4;
+                row[6] = star3 - 0;
+                row[7] = (ull)(sv * su) - c4;
+            }
+        }
+#pragma omp critical
+        for (int k = 0; k < PO_NSUMS; k++) total[k] += loc[k];
+        free(ind); free(T); free(S);
+    }
+    free(vol2);
+    memcpy(g->sums, total, sizeof(total));
+    po_close(g->sums, n, m, g->totals);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+int64_t po_n(const po_graph *g) { return g->n; }
+int64_t po_m(const po_graph *g) { return g->m; }
+int po_max_degree(const po_graph *g) { return g->max_degree; }
+int po_max_core(const po_graph *g) { return g->max_core; }
+void po_get_csr(const po_graph *g, int64_t *off, int32_t *adj) {
+    memcpy(off, g->off, (size_t)(g->n + 1) * sizeof(int64_t));
+    memcpy(adj, g->adj, (size_t)g->off[g->n] * sizeof(int32_t));
+}
+void po_get_edges(const po_graph *g, int64_t *ev, int64_t *eu) {
+    memcpy(ev, g->ev, (size_t)g->n_e * sizeof(int64_t));
+    memcpy(eu, g->eu, (size_t)g->n_e * sizeof(int64_t));
+}
+void po_get_order(const po_graph *g, int32_t *ids) { memcpy(ids, g->ord, (size_t)g->n_ord * sizeof(int32_t)); }
+void po_get_kcore(const po_graph *g, int32_t *kc) { memcpy(kc, g->kcore, (size_t)(g->n + 1) * sizeof(int32_t)); }
+void po_get_sums(const po_graph *g, uint64_t *s) { memcpy(s, g->sums, sizeof(g->sums)); }
+void po_get_totals(const po_graph *g, uint64_t *t) { memcpy(t, g->totals, sizeof(g->totals)); }
+void po_get_micro(const po_graph *g, int64_t *src1, int64_t *dst1, uint64_t *cols) {
+    for (int64_t e = 0; e < g->n_ord; e++) {
+        int32_t id = g->ord[e];
+        src1[e] = g->ev[id] + 1;
+        dst1[e] = g->eu[id] + 1;
+    }
+    if (g->micro) memcpy(cols, g->micro, (size_t)g->n_ord * PO_NMICRO * sizeof(uint64_t));
+}
+void po_get_edge_tkc(const po_graph *g, uint64_t *t, uint64_t *k4, uint64_t *c4) {
+    memcpy(t, g->t_e, (size_t)g->n_e * sizeof(uint64_t));
+    memcpy(k4, g->k4_e, (size_t)g->n_e * sizeof(uint64_t));
+    memcpy(c4, g->c4_e, (size_t)g->n_e * sizeof(uint64_t));
+}
