@@ -1,0 +1,373 @@
+#!/usr/bin/env python3
+"""Benchmark: exact 3/4-node graphlet decomposition of an RMAT scale-20 graph.
+
+Workload (the reference's headline shape): RMAT scale 20, edge factor 16,
+(a, b, c, d) = (0.57, 0.19, 0.19, 0.05), seed 1, symmetrised, deduplicated,
+self loops dropped; degeneracy (k-core) edge ordering; the 17 global counts
+plus the 8 per-edge counts of every edge.  Metric: edges/s.
+
+One step = sort_edges("kcore") + decomposition (global + per-edge) of the
+HBM-resident graph, i.e. the span the reference times as "graphlet
+decomposition time" (graphlet_driver.cpp:67-78).  L2 is flushed before every
+step by a 256 MB device write.  `e2e` runs the same metric through the public
+API from pinned host buffers: upload of the raw pairs, device CSR build,
+ordering, k-core, decomposition and the copy of all per-edge rows back.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With N > 1 (torchrun) every rank decomposes its own copy of the workload
+(independent graphs, no collective on the data path): weak scaling.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "edges/s full 4-node counts (bit-exact)"
+UNIT = "edges/s"
+RMAT = dict(a=0.57, b=0.19, c=0.19)
+
+# DRAM traffic of one k_decompose launch on this workload, from the ncu
+# capture summarised in profiles/ (None until a capture exists).
+NCU_TRAFFIC_BYTES = None
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload_config(scale, order, n=None, m=None):
+    cfg = {
+        "workload": "rmat%d_%s_global+micro" % (scale, order),
+        "graph": "RMAT scale %d, edge factor 16, (a,b,c,d)=(0.57,0.19,0.19,0.05), seed 1, symmetrised, "
+                 "deduplicated, self loops dropped" % scale,
+        "ordering": "%s edge order (degeneracy)" % order if order == "kcore" else order,
+        "counts": "17 global (uint64) + 8 per-edge columns for every edge",
+        "step": "sort_edges + decomposition on the HBM-resident CSR",
+        "l2": "flushed before every step (256 MB device write)",
+    }
+    if n is not None:
+        cfg["n"] = int(n)
+        cfg["m"] = int(m)
+    return cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.out = ""
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            self.out = ""
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def algorithmic_bytes(ev, eu, n, micro=True):
+    """Bytes an edge-centric decomposition must stream: per edge both
+    endpoint lists plus the 2-hop lists of the cheaper endpoint, 4 B per
+    adjacency entry, plus 64 B of per-edge output (micro)."""
+    deg = np.bincount(ev, minlength=n) + np.bincount(eu, minlength=n)
+    vol2 = np.bincount(ev, weights=deg[eu], minlength=n) + np.bincount(eu, weights=deg[ev], minlength=n)
+    entries = (deg[ev] + deg[eu]).sum(dtype=np.float64) + np.minimum(vol2[ev], vol2[eu]).sum(dtype=np.float64)
+    return 4.0 * entries + (64.0 * len(ev) if micro else 0.0)
+
+
+def cpu_sample(src, dst, order, target_s, threads):
+    """Edges/s of the reference's per-edge loop on the host cores over a
+    bounded, evenly spaced sample of the ordered edges.  Uses the reference
+    compiled from its sources where present (oracle/_ref), else the oracle
+    port of it (same algorithm: mark e_v, scan e_u's 2-hop lists)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as ol
+
+    og = ol.OracleGraph.from_pairs(src, dst, dedup=True)
+    m = og.m
+    kind = "port"
+    runner = None
+    if ol.ref_available():
+        try:
+            off, adj = og.csr()
+            rg = ol.RefGraph.from_csr(off, adj)
+            kind = "reference"
+
+            def runner(stride):
+                return rg.time_sample(stride, order=order, workers=threads)
+        except OSError:
+            runner = None
+    if runner is None:
+        og.prepare(order=order)
+
+        def runner(stride):
+            return og.time_sample(stride, threads=threads)
+
+    stride = max(1, m // 256)
+    k, sec = runner(stride)
+    # grow the sample toward target_s seconds
+    while sec < target_s / 4 and stride > 1:
+        stride = max(1, int(stride * max(sec, 1e-3) / target_s))
+        k, sec = runner(stride)
+    return kind, k, sec, stride, m
+
+
+def run_reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import pgd_gb300 as pgd
+
+    threads = os.cpu_count() or 1
+    src, dst = pgd.rmat(args.scale, 16, seed=1, **RMAT)
+    target = args.cpu_seconds
+    per = []
+    kind = None
+    total_e, total_s = 0, 0.0
+    for step in range(args.warmup + args.steps):
+        kind, k, sec, stride, m = cpu_sample(src, dst, args.order, target, threads)
+        if step >= args.warmup:
+            total_e += k
+            total_s += sec
+            per.append(sec)
+    value = total_e / total_s
+    sample = "every %d-th edge of the %s order (%d of %d edges) per step" % (stride, args.order, k, m)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / max(1, args.steps),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded RMAT generator)", "config": workload_config(args.scale, args.order),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scale", type=int, default=20)
+    ap.add_argument("--order", default="kcore")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+
+    import torch
+
+    import pgd_gb300 as pgd
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- input (host) and graph (device) ----------------------------------
+    t0 = time.time()
+    src, dst = pgd.rmat(args.scale, 16, seed=1, **RMAT)
+    log("rank %d: generated %d pairs in %.1fs" % (rank, len(src), time.time() - t0))
+    stream = torch.cuda.Stream(device=dev)
+    ctx = pgd.Context(device=local, stream=stream.cuda_stream)
+    t0 = time.time()
+    g = ctx.graph_from_edges(src, dst, dedup=True)
+    g.preprocess("deg")
+    K = g.compute_cores()
+    info = g.info()
+    n, m = info.n, info.m
+    log("rank %d: graph n=%d m=%d dmax=%d K=%d built in %.2fs" % (rank, n, m, info.max_degree, K, time.time() - t0))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step():
+        g.sort_edges(args.order)
+        return g.decompose(micro=True)
+
+    ref_totals = None
+    for w in range(args.warmup):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        r = step()
+        log("rank %d: warmup %d kernel %.1f ms" % (rank, w, r.kernel_ms))
+        if ref_totals is None:
+            ref_totals = r.totals.copy()
+        assert (r.totals == ref_totals).all(), "decomposition not repeatable"
+
+    # ---- timed region ------------------------------------------------------
+    clocks = ClockSampler(local)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    kernel_ms = []
+    launches0 = ctx.kernel_launches
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        r = step()
+        kernel_ms.append(r.kernel_ms)
+        if ref_totals is not None:
+            assert (r.totals == ref_totals).all(), "decomposition not repeatable"
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    launches = ctx.kernel_launches - launches0
+    window_ms = max_over_ranks(ev0.elapsed_time(ev1))
+    value = world * m * args.steps / (window_ms / 1000.0)
+    ms_per_step = window_ms / args.steps
+    log("rank %d: %.1f ms/step, kernel %.1f ms, %.3g edges/s" % (rank, ms_per_step, np.mean(kernel_ms), value))
+
+    # ---- roofline of the decomposition kernel -----------------------------
+    ev, eu, _ = g.edges(with_order=False)
+    b_alg = algorithmic_bytes(ev, eu, n, micro=True)
+    kern_s = float(np.mean(kernel_ms)) / 1000.0
+    peak, peak_src = peaks()
+    achieved = b_alg / kern_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": NCU_TRAFFIC_BYTES, "kernel": "k_decompose", "kernel_ms": float(np.mean(kernel_ms)),
+                "algorithmic_bytes": b_alg, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)"
+                if peak_src == "measured" else "fallback 6.8 TB/s"}
+
+    # ---- end to end through the public API --------------------------------
+    e2e = None
+    if not args.no_e2e:
+        h_src = torch.from_numpy(src).pin_memory().numpy()
+        h_dst = torch.from_numpy(dst).pin_memory().numpy()
+        h_cols = torch.empty((m, pgd.NMICRO), dtype=torch.int64).pin_memory().numpy().view(np.uint64)
+        h_s1 = torch.empty(m, dtype=torch.int64).pin_memory().numpy()
+        h_d1 = torch.empty(m, dtype=torch.int64).pin_memory().numpy()
+
+        def e2e_step():
+            ge = ctx.graph_from_edges(h_src, h_dst, dedup=True)
+            ge.preprocess("deg")
+            ge.compute_cores()
+            ge.sort_edges(args.order)
+            res = ge.decompose(micro=True)
+            lib = pgd.lib()
+            st = lib.pgd_get_micro(ge.h, pgd._ptr(h_s1), pgd._ptr(h_d1), pgd._ptr(h_cols))
+            assert st == 0
+            ge.destroy()
+            return res
+
+        e2e_step()
+        barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.e2e_steps):
+            res = e2e_step()
+            assert (res.totals == ref_totals).all()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        e2e_ms = max_over_ranks(e0.elapsed_time(e1)) / args.e2e_steps
+        e2e = {"value": world * m / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
+               "h2d_bytes_per_step": int(src.nbytes + dst.nbytes),
+               "d2h_bytes_per_step": int(m * (pgd.NMICRO * 8 + 12) + (pgd.NTOTALS + pgd.NSUMS) * 8)}
+        log("rank %d: e2e %.1f ms/step" % (rank, e2e_ms))
+
+    # ---- CPU baseline (rank 0, N = 1) ---------------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        kind, k, sec, stride, _ = cpu_sample(src, dst, args.order, args.cpu_seconds, threads)
+        cpu = {"value": k / sec, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": "every %d-th edge of the %s order: %d of %d edges, global counts, %.1f s" %
+                         (stride, args.order, k, m, sec)}
+        log("cpu baseline (%s, %d threads): %.3g edges/s" % (kind, threads, k / sec))
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded RMAT generator)",
+            "config": workload_config(args.scale, args.order, n, m), "roofline": roofline,
+            "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
+            "totals": {k_: int(v) for k_, v in zip(pgd.TOTAL_NAMES, ref_totals)},
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -782,6 +782,71 @@ int po_decompose(po_graph *g, int micro, int threads, int cheap_side) {
     return 0;
 }
 
+int64_t po_decompose_sample(po_graph *g, int threads, int cheap_side, int64_t stride, double *seconds) {
+    if (!g->ord) { if (po_sort_edges(g, "deg", 0)) return -1; }
+    if (stride < 1) stride = 1;
+    int64_t n = g->n, m = g->m, ne = (g->n_ord + stride - 1) / stride;
+    ull *vol2 = NULL;
+    if (cheap_side) {
+        vol2 = malloc((size_t)(n + 1) * sizeof(ull));
+        for (int64_t x = 0; x < n; x++) {
+            ull s = 0;
+            for (int64_t j = g->off[x]; j < g->off[x + 1]; j++) s += (ull)g->deg[g->adj[j]];
+            vol2[x] = s;
+        }
+    }
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+    double t0 = omp_get_wtime();
+#endif
+    ull total[PO_NSUMS];
+    memset(total, 0, sizeof(total));
+#pragma omp parallel
+    {
+        uint8_t *ind = calloc((size_t)n + 1, 1);
+        int32_t *T = malloc((size_t)(g->max_degree + 1) * sizeof(int32_t));
+        int32_t *S = malloc((size_t)(g->max_degree + 1) * sizeof(int32_t));
+        ull loc[PO_NSUMS];
+        memset(loc, 0, sizeof(loc));
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t i = 0; i < ne; i++) {
+            int32_t id = g->ord[i * stride];
+            long long v = g->ev[id], u = g->eu[id];
+            long long a = v, b = u;
+            if (cheap_side && vol2[u] > vol2[v]) { a = u; b = v; }
+            for (int64_t j = g->off[a]; j < g->off[a + 1]; j++) if (g->adj[j] != b) ind[g->adj[j]] = 1;
+            ull t = 0, ns = 0;
+            for (int64_t j = g->off[b]; j < g->off[b + 1]; j++) {
+                int32_t w = g->adj[j];
+                if (w == a) continue;
+                if (ind[w] == 1) { ind[w] = 3; T[t++] = w; }
+                else { S[ns++] = w; }
+            }
+            edge_sums(loc, g->deg[v], g->deg[u], t, m, n);
+            ull c4 = 0, k4 = 0;
+            for (ull k = 0; k < ns; k++)
+                for (int64_t j = g->off[S[k]]; j < g->off[S[k] + 1]; j++) c4 += (ind[g->adj[j]] == 1);
+            for (ull k = 0; k < t; k++) {
+                for (int64_t j = g->off[T[k]]; j < g->off[T[k] + 1]; j++) k4 += (ind[g->adj[j]] == 3);
+                ind[T[k]] = 0;
+            }
+            for (int64_t j = g->off[a]; j < g->off[a + 1]; j++) ind[g->adj[j]] = 0;
+            loc[3] += k4;
+            loc[4] += c4;
+        }
+#pragma omp critical
+        for (int k = 0; k < PO_NSUMS; k++) total[k] += loc[k];
+        free(ind); free(T); free(S);
+    }
+#ifdef _OPENMP
+    if (seconds) *seconds = omp_get_wtime() - t0;
+#else
+    if (seconds) *seconds = 0;
+#endif
+    free(vol2);
+    return ne;
+}
+
 /* ------------------------------------------------------------------------ */
 int64_t po_n(const po_graph *g) { return g->n; }
 int64_t po_m(const po_graph *g) { return g->m; }

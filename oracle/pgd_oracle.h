@@ -54,6 +54,12 @@ int po_sort_edges(po_graph *g, const char *order, int s2l);
  * volume instead of always e_u (same counts, less work on power-law graphs). */
 int po_decompose(po_graph *g, int micro, int threads, int cheap_side);
 
+/* Timing sample for the CPU baseline: runs the per-edge loop (global
+ * counts) over E_ordered positions 0, stride, 2*stride, ... with all or
+ * `threads` threads and returns the number of edges done; *seconds gets the
+ * wall time of the loop alone.  Results are not kept. */
+int64_t po_decompose_sample(po_graph *g, int threads, int cheap_side, int64_t stride, double *seconds);
+
 /* Closing identities (graphlet_core.cpp:1449-1472, graphlet_core.h:548-557). */
 void po_close(const uint64_t sums[PO_NSUMS], int64_t n, int64_t m, uint64_t totals[PO_NTOTALS]);
 

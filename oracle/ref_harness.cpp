@@ -25,10 +25,14 @@ void *ref_open_file(const char *path, const char *neigh, int s2l_neigh, int adj_
 
 void *ref_open_csr(int64_t n, const int64_t *off, const int32_t *adj, const char *neigh, int s2l_neigh,
                    int adj_limit, const char *rep) {
-    std::vector<long long> vs(off, off + n + 1);
-    std::vector<int> es(adj, adj + off[n]);
-    graphlet_core *g = new graphlet_core(vs, es);
+    // The CSR constructor (graphlet_core.h:156-160) runs vertex_degrees()
+    // before initialize() has set block_size, so its OpenMP loop sees an
+    // uninitialised chunk size.  The same state is reached without that by
+    // the default constructor, initialize(), and the public CSR fields.
+    graphlet_core *g = new graphlet_core();
     g->initialize();
+    g->vertices.assign(off, off + n + 1);
+    g->edges.assign(adj, adj + off[n]);
     g->vertex_degrees();
     g->preprocess(std::string(neigh), s2l_neigh != 0, adj_limit, std::string(rep));
     return g;
@@ -43,6 +47,25 @@ int ref_run(void *h, const char *order, int s2l, int micro, int workers) {
     if (micro) g->graphlet_decomposition_micro(workers);
     else g->graphlet_decomposition(workers);
     return 0;
+}
+
+// Timing sample for the CPU baseline: the reference's own sampled edge order
+// (sort_edges over a subset E_s, graphlet_core.cpp:837-851) holding every
+// stride-th edge of the full order, then its decomposition over that subset.
+// Returns the number of edges; *seconds is the decomposition's wall time.
+long long ref_run_sample(void *h, const char *order, int s2l, int workers, long long stride, double *seconds) {
+    graphlet_core *g = (graphlet_core *)h;
+    g->compute_cores();
+    g->E_ordered.clear();
+    g->sort_edges(std::string(order), s2l != 0);
+    std::vector<unsigned long> sample;
+    for (size_t i = 0; i < g->E_ordered.size(); i += (size_t)stride) sample.push_back(g->E_ordered[i].get_id());
+    g->E_ordered.clear();
+    g->sort_edges(std::string(order), s2l != 0, sample);
+    double t0 = get_time();
+    g->graphlet_decomposition(workers);
+    *seconds = get_time() - t0;
+    return (long long)sample.size();
 }
 
 void ref_totals(void *h, uint64_t *out) {

@@ -1,0 +1,380 @@
+// api.cpp -- the C ABI entry points (include/pgd_gb300.h): context and graph
+// lifetime, option parsing, host<->device copies of results.  Compute is in
+// graph_build.cu and decompose.cu; nothing here computes counts on the CPU.
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "pgd_internal.h"
+#include "pgd_reader.h"
+
+// ---------------------------------------------------------------------------
+// errors and memory
+
+pgd_status pgd_fail(pgd_ctx *ctx, pgd_status s, const std::string &msg) {
+    if (ctx) ctx->err = msg;
+    return s;
+}
+
+pgd_status pgd_cuda_fail(pgd_ctx *ctx, cudaError_t e, const char *what) {
+    std::string msg = std::string("CUDA error ") + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ") in " + what;
+    if (e == cudaErrorMemoryAllocation) return pgd_fail(ctx, PGD_ENOMEM, msg);
+    return pgd_fail(ctx, PGD_ECUDA, msg);
+}
+
+pgd_status pgd_graph_alloc(pgd_graph *g, void **p, size_t bytes) {
+    pgd_ctx *ctx = g->ctx;
+    if (ctx->resident + bytes > ctx->budget)
+        return pgd_fail(ctx, PGD_ENOMEM, "HBM budget of the context exceeded (" + std::to_string(ctx->resident + bytes) +
+                                             " > " + std::to_string(ctx->budget) + " bytes)");
+    cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 16, ctx->stream);
+    if (e != cudaSuccess) { cudaGetLastError(); return pgd_cuda_fail(ctx, e, "cudaMallocAsync"); }
+    ctx->resident += bytes;
+    g->bytes += bytes;
+    return PGD_OK;
+}
+
+void pgd_graph_free(pgd_graph *g, void *p, size_t bytes) {
+    if (!p) return;
+    cudaFreeAsync(p, g->ctx->stream);
+    g->ctx->resident -= bytes;
+    g->bytes -= bytes;
+}
+
+pgd_status pgd_tmp_alloc(pgd_ctx *ctx, void **p, size_t bytes) {
+    cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 16, ctx->stream);
+    if (e != cudaSuccess) { cudaGetLastError(); return pgd_cuda_fail(ctx, e, "cudaMallocAsync (temporary)"); }
+    return PGD_OK;
+}
+
+void pgd_tmp_free(pgd_ctx *ctx, void *p) {
+    if (p) cudaFreeAsync(p, ctx->stream);
+}
+
+// ---------------------------------------------------------------------------
+// context
+
+extern "C" const char *pgd_status_string(pgd_status s) {
+    switch (s) {
+    case PGD_OK: return "ok";
+    case PGD_EINVAL: return "invalid argument or input";
+    case PGD_ENOMEM: return "out of memory or over budget";
+    case PGD_ETIMEOUT: return "bounded device wait timed out";
+    case PGD_ECUDA: return "CUDA error";
+    case PGD_EIO: return "I/O error";
+    case PGD_EUNSUPPORTED: return "unsupported option";
+    }
+    return "unknown status";
+}
+
+extern "C" pgd_status pgd_context_create(const pgd_opts *opts, pgd_ctx **out) {
+    if (!out) return PGD_EINVAL;
+    *out = nullptr;
+    pgd_opts o;
+    memset(&o, 0, sizeof(o));
+    if (opts) o = *opts;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) { cudaGetLastError(); return PGD_ECUDA; }
+    if (o.device < 0 || o.device >= count) return PGD_EINVAL;
+    if (cudaSetDevice(o.device) != cudaSuccess) return PGD_ECUDA;
+    pgd_ctx *ctx = new pgd_ctx();
+    ctx->device = o.device;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, o.device) != cudaSuccess) { delete ctx; return PGD_ECUDA; }
+    ctx->num_sms = prop.multiProcessorCount;
+    if (o.stream) {
+        ctx->stream = (cudaStream_t)o.stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return PGD_ECUDA; }
+        ctx->own_stream = true;
+    }
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    ctx->budget = o.hbm_budget ? o.hbm_budget : (uint64_t)(0.9 * (double)free_b);
+    // keep freed pool memory cached: graph builds reuse it
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, o.device) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    if (cudaMalloc((void **)&ctx->d_sums, 64 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc((void **)&ctx->d_ctr, 64 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+        cudaGetLastError();
+        pgd_context_destroy(ctx);
+        return PGD_ECUDA;
+    }
+    *out = ctx;
+    return PGD_OK;
+}
+
+extern "C" pgd_status pgd_context_destroy(pgd_ctx *ctx) {
+    if (!ctx) return PGD_EINVAL;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->d_sums) cudaFree(ctx->d_sums);
+    if (ctx->d_ctr) cudaFree(ctx->d_ctr);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return PGD_OK;
+}
+
+extern "C" const char *pgd_last_error(const pgd_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+extern "C" uint64_t pgd_context_resident_bytes(const pgd_ctx *ctx) { return ctx ? ctx->resident : 0; }
+
+extern "C" uint64_t pgd_context_kernel_launches(const pgd_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+// ---------------------------------------------------------------------------
+// graphs
+
+static pgd_graph *new_graph(pgd_ctx *ctx) {
+    pgd_graph *g = new pgd_graph();
+    g->ctx = ctx;
+    return g;
+}
+
+extern "C" pgd_status pgd_graph_destroy(pgd_graph *g) {
+    if (!g) return PGD_EINVAL;
+    cudaSetDevice(g->ctx->device);
+    pgd_graph_free(g, g->off, (g->n + 1) * sizeof(int64_t));
+    pgd_graph_free(g, g->adj, (2 * g->m + 1) * sizeof(int32_t));
+    pgd_graph_free(g, g->rank, (2 * g->m + 1) * sizeof(int64_t));
+    pgd_graph_free(g, g->deg, (g->n + 1) * sizeof(int32_t));
+    pgd_graph_free(g, g->vol2, (g->n + 1) * sizeof(uint64_t));
+    pgd_graph_free(g, g->ev, (g->m + 1) * sizeof(int32_t));
+    pgd_graph_free(g, g->eu, (g->m + 1) * sizeof(int32_t));
+    pgd_graph_free(g, g->core, (g->n + 1) * sizeof(int32_t));
+    pgd_graph_free(g, g->order, (g->m + 1) * sizeof(int32_t));
+    pgd_graph_free(g, g->micro, (g->m + 1) * PGD_NMICRO * sizeof(uint64_t));
+    // whatever is left (partial builds) is returned to the budget as well
+    g->ctx->resident -= g->bytes;
+    cudaStreamSynchronize(g->ctx->stream);
+    delete g;
+    return PGD_OK;
+}
+
+static pgd_status finish_new(pgd_graph *g, pgd_status st, pgd_graph **out) {
+    if (st != PGD_OK) {
+        pgd_graph_destroy(g);
+        return st;
+    }
+    *out = g;
+    return PGD_OK;
+}
+
+extern "C" pgd_status pgd_graph_from_edges(pgd_ctx *ctx, const int32_t *src, const int32_t *dst, int64_t k,
+                                           int64_t n_min, uint32_t flags, pgd_graph **out) {
+    if (!ctx || !out || k < 0 || (k > 0 && (!src || !dst)) || n_min < 0) return pgd_fail(ctx, PGD_EINVAL, "bad arguments");
+    cudaSetDevice(ctx->device);
+    pgd_graph *g = new_graph(ctx);
+    return finish_new(g, pgd_build_from_pairs(g, src, dst, k, n_min, (flags & PGD_EDGES_DEDUP) != 0), out);
+}
+
+extern "C" pgd_status pgd_graph_from_csr(pgd_ctx *ctx, const int64_t *off, const int32_t *adj, int64_t n,
+                                         pgd_graph **out) {
+    if (!ctx || !out || !off || n < 0 || (off[n] > 0 && !adj)) return pgd_fail(ctx, PGD_EINVAL, "bad arguments");
+    cudaSetDevice(ctx->device);
+    pgd_graph *g = new_graph(ctx);
+    return finish_new(g, pgd_build_from_csr(g, off, adj, n), out);
+}
+
+extern "C" pgd_status pgd_graph_from_file(pgd_ctx *ctx, const char *path, pgd_graph **out) {
+    if (!ctx || !out || !path) return pgd_fail(ctx, PGD_EINVAL, "bad arguments");
+    ReadResult r;
+    if (!pgd_read_graph_file(path, r)) {
+        bool missing = r.error.rfind("file not found", 0) == 0;
+        return pgd_fail(ctx, missing ? PGD_EIO : PGD_EINVAL, r.error);
+    }
+    pgd_status st = pgd_graph_from_edges(ctx, r.src.data(), r.dst.data(), (int64_t)r.src.size(), 0,
+                                         r.is_mtx ? 0u : PGD_EDGES_DEDUP, out);
+    if (st == PGD_OK) (*out)->self_loops = r.self_loops;
+    if (st == PGD_EINVAL && r.is_mtx && ctx->err.find("repeated pair") != std::string::npos)
+        ctx->err = "mtx file lists an edge twice; the reference does not deduplicate mtx input and its counts "
+                   "are undefined for multigraphs";
+    return st;
+}
+
+extern "C" pgd_status pgd_graph_info(const pgd_graph *g, pgd_info *info) {
+    if (!g || !info) return PGD_EINVAL;
+    info->n = g->n;
+    info->m = g->m;
+    info->max_degree = g->max_degree;
+    info->avg_degree = g->n ? (int32_t)((double)(2 * g->m) / (double)g->n) : 0;
+    info->self_loops = g->self_loops;
+    info->duplicates = g->duplicates;
+    return PGD_OK;
+}
+
+extern "C" uint64_t pgd_graph_resident_bytes(const pgd_graph *g) { return g ? g->bytes : 0; }
+
+// ---------------------------------------------------------------------------
+// ordering
+
+static int parse_neigh(const char *s) {
+    std::string o = s ? s : "";
+    if (o == "degree" || o == "deg") return PGD_NEIGH_DEG;
+    if (o == "kcore") return PGD_NEIGH_KCORE;
+    static const char *unsupported[] = {"rand", "degree_kcore", "deg_kcore", "degree_vol", "deg_vol",
+                                        "kcore_vol", "degree_kcore_vol", "deg_kcore_vol"};
+    for (const char *u : unsupported)
+        if (o == u) return -1;
+    return PGD_NEIGH_ASREAD;
+}
+
+static int parse_order(const char *s) {
+    std::string o = s ? s : "";
+    if (o == "natural") return PGD_ORD_NATURAL;
+    if (o == "deg" || o == "degree") return PGD_ORD_DEG;
+    if (o == "kcore" || o == "kcores") return PGD_ORD_KCORE;
+    if (o == "kcore_deg" || o == "kcore_degree") return PGD_ORD_KCORE_DEG;
+    if (o == "deg_vol" || o == "degree_vol") return PGD_ORD_DEG_VOL;
+    if (o == "kcore_vol" || o == "kcore_volume") return PGD_ORD_KCORE_VOL;
+    if (o == "kcore_deg_vol" || o == "kcore_degree_vol") return PGD_ORD_KCORE_DEG_VOL;
+    if (o == "rand" || o == "random" || o == "var") return -1;
+    // names the reference maps to enum values past VAR use the default
+    // branch of get_ordering_value (graphlet_core.cpp:829-832)
+    static const char *deg_u[] = {
+        "triangles", "tri", "triangle", "wedges", "tcores", "triangle_cores", "triangle_core", "tcore", "coloring",
+        "greedy_coloring", "tri_vol", "triangle_vol", "tcore_vol", "tcore_volume", "triangle_core_vol",
+        "triangles_only", "triangle_only", "dynamic_largest_first", "lfo", "LFO", "triangle_core_max", "tcore_max",
+        "tcores_max", "degree_triangles", "degree_tri", "deg_tri", "deg_triangles", "kcore_tri", "kcore_triangles",
+        "kcore_triangle", "kcore_deg_tri", "kcore_degree_triangle", "kcore_degree_tri", "kcore_tri_vol",
+        "kcore_triangle_vol", "kcore_deg_tri_vol", "kcore_degree_tri_vol", "dist_two_lfo", "dist_two_largest_first",
+        "dist_two_dlfo", "dist_two_dynamic_lfo", "dist_two_slo", "dist_two_smallest_last", "ido", "incidence",
+        "incidence_deg", "dist_two_ido", "dist_two_incidence", "dist_two_tcore", "dist_two_triangle_core",
+        "tcore_min", "triangle_core_min", "tri_core_min", "common", "common_neighbors"};
+    for (const char *d : deg_u)
+        if (o == d) return PGD_ORD_DEG_U;
+    return PGD_ORD_NATURAL;
+}
+
+extern "C" pgd_status pgd_compute_cores(pgd_graph *g, int32_t *max_core) {
+    if (!g) return PGD_EINVAL;
+    cudaSetDevice(g->ctx->device);
+    if (!g->has_cores) {
+        pgd_status st = pgd_dev_cores(g);
+        if (st) return st;
+    }
+    if (max_core) *max_core = g->max_core;
+    return PGD_OK;
+}
+
+extern "C" pgd_status pgd_get_kcore(pgd_graph *g, int32_t *kcore) {
+    if (!g || !kcore) return PGD_EINVAL;
+    pgd_status st = pgd_compute_cores(g, nullptr);
+    if (st) return st;
+    kcore[0] = 0;
+    if (g->n) PGD_CUDA(g->ctx, cudaMemcpy(kcore + 1, g->core, g->n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return PGD_OK;
+}
+
+extern "C" pgd_status pgd_preprocess(pgd_graph *g, const char *neigh_order, int small_to_large) {
+    if (!g) return PGD_EINVAL;
+    cudaSetDevice(g->ctx->device);
+    int kind = parse_neigh(neigh_order);
+    if (kind < 0)
+        return pgd_fail(g->ctx, PGD_EUNSUPPORTED,
+                        std::string("neighbour ordering '") + (neigh_order ? neigh_order : "") +
+                            "' is not deterministic or not well defined in the reference");
+    if (kind == PGD_NEIGH_KCORE && !g->has_cores) {
+        pgd_status st = pgd_dev_cores(g);
+        if (st) return st;
+    }
+    return pgd_dev_preprocess(g, kind, small_to_large);
+}
+
+extern "C" pgd_status pgd_assortativity(pgd_graph *g, double *r) {
+    if (!g || !r) return PGD_EINVAL;
+    cudaSetDevice(g->ctx->device);
+    if (!g->preprocessed) {
+        pgd_status st = pgd_preprocess(g, "deg", 0);
+        if (st) return st;
+    }
+    return pgd_dev_assortativity(g, r);
+}
+
+extern "C" pgd_status pgd_sort_edges(pgd_graph *g, const char *order, int small_to_large) {
+    if (!g) return PGD_EINVAL;
+    cudaSetDevice(g->ctx->device);
+    int kind = parse_order(order);
+    if (kind < 0)
+        return pgd_fail(g->ctx, PGD_EUNSUPPORTED,
+                        std::string("edge ordering '") + (order ? order : "") +
+                            "' is wall-clock seeded or divides by zero in the reference");
+    pgd_status st;
+    if (!g->preprocessed && (st = pgd_preprocess(g, "deg", 0))) return st;
+    bool need_cores = kind == PGD_ORD_KCORE || kind == PGD_ORD_KCORE_DEG || kind == PGD_ORD_KCORE_VOL ||
+                      kind == PGD_ORD_KCORE_DEG_VOL;
+    if (need_cores && !g->has_cores && (st = pgd_dev_cores(g))) return st;
+    return pgd_dev_sort_edges(g, kind, small_to_large);
+}
+
+// ---------------------------------------------------------------------------
+// decomposition and results
+
+extern "C" pgd_status pgd_decompose(pgd_graph *g, uint32_t flags, pgd_counts *out) {
+    if (!g || !out) return PGD_EINVAL;
+    cudaSetDevice(g->ctx->device);
+    pgd_status st;
+    memset(out, 0, sizeof(*out));
+    if (!g->preprocessed && (st = pgd_preprocess(g, "deg", 0))) return st;
+    if (!g->sorted && (st = pgd_sort_edges(g, "deg", 0))) return st;
+    return pgd_dev_decompose(g, (flags & PGD_MICRO) != 0, out);
+}
+
+extern "C" pgd_status pgd_get_edges(pgd_graph *g, int64_t *ev, int64_t *eu, int32_t *order) {
+    if (!g) return PGD_EINVAL;
+    if (!g->preprocessed) return pgd_fail(g->ctx, PGD_EINVAL, "graph is not preprocessed");
+    cudaSetDevice(g->ctx->device);
+    std::vector<int32_t> tmp((size_t)g->m + 1);
+    if (ev) {
+        PGD_CUDA(g->ctx, cudaMemcpy(tmp.data(), g->ev, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < g->m; i++) ev[i] = tmp[i];
+    }
+    if (eu) {
+        PGD_CUDA(g->ctx, cudaMemcpy(tmp.data(), g->eu, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < g->m; i++) eu[i] = tmp[i];
+    }
+    if (order) {
+        if (!g->sorted) return pgd_fail(g->ctx, PGD_EINVAL, "edges are not sorted");
+        PGD_CUDA(g->ctx, cudaMemcpy(order, g->order, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    }
+    return PGD_OK;
+}
+
+extern "C" pgd_status pgd_get_micro(pgd_graph *g, int64_t *src1, int64_t *dst1, uint64_t *cols) {
+    if (!g) return PGD_EINVAL;
+    if (!g->has_micro) return pgd_fail(g->ctx, PGD_EINVAL, "no per-edge results: decompose with PGD_MICRO first");
+    cudaSetDevice(g->ctx->device);
+    if (cols && g->m)
+        PGD_CUDA(g->ctx, cudaMemcpy(cols, g->micro, g->m * PGD_NMICRO * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    if (src1 || dst1) {
+        std::vector<int32_t> ev((size_t)g->m + 1), eu((size_t)g->m + 1), ord((size_t)g->m + 1);
+        if (g->m) {
+            PGD_CUDA(g->ctx, cudaMemcpy(ev.data(), g->ev, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
+            PGD_CUDA(g->ctx, cudaMemcpy(eu.data(), g->eu, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
+            PGD_CUDA(g->ctx, cudaMemcpy(ord.data(), g->order, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        }
+        for (int64_t e = 0; e < g->m; e++) {
+            if (src1) src1[e] = (int64_t)ev[ord[e]] + 1;
+            if (dst1) dst1[e] = (int64_t)eu[ord[e]] + 1;
+        }
+    }
+    return PGD_OK;
+}
+
+extern "C" pgd_status pgd_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k, uint32_t flags,
+                                          pgd_counts *out) {
+    if (!ctx || k < 0 || (k > 0 && (!graphs || !out))) return pgd_fail(ctx, PGD_EINVAL, "bad arguments");
+    for (int i = 0; i < k; i++) {
+        pgd_status st = pgd_decompose(graphs[i], flags, &out[i]);
+        if (st) return st;
+    }
+    return PGD_OK;
+}

@@ -1,0 +1,106 @@
+// pgd_internal.h -- state behind the C ABI (include/pgd_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "pgd_gb300.h"
+
+struct pgd_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    uint64_t budget = 0;     // bytes graphs of this context may hold
+    uint64_t resident = 0;   // bytes currently held
+    std::string err;
+    // decomposition scratch: per-launch counters and sums
+    unsigned long long *d_sums = nullptr;   // PGD_NSUMS
+    unsigned long long *d_ctr = nullptr;    // work counters
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    unsigned long long launches = 0;        // kernels of this library launched
+};
+
+struct pgd_graph {
+    pgd_ctx *ctx = nullptr;
+    int64_t n = 0, m = 0;
+    int32_t max_degree = 0;
+    int64_t self_loops = 0, duplicates = 0;
+    uint64_t bytes = 0;               // device bytes held
+
+    // compute CSR: rows sorted by neighbour id
+    int64_t *off = nullptr;           // n+1
+    int32_t *adj = nullptr;           // 2m
+    int32_t *deg = nullptr;           // n
+    int64_t *rank = nullptr;          // 2m insertion rank of each entry
+    uint64_t *vol2 = nullptr;         // n: sum of neighbour degrees
+
+    // preprocess: edge arrays by edge id (graphlet_core.cpp:929-949)
+    bool preprocessed = false;
+    int32_t *ev = nullptr, *eu = nullptr;   // m
+
+    // cores (0-based core numbers)
+    bool has_cores = false;
+    int32_t *core = nullptr;          // n
+    int32_t max_core = 0;
+
+    // E_ordered edge ids
+    bool sorted = false;
+    int32_t *order = nullptr;         // m
+
+    // per-edge results in E_ordered order
+    bool has_micro = false;
+    uint64_t *micro = nullptr;        // m * 8
+};
+
+// Launch one of this library's kernels on the context's stream and count it.
+#define PGD_LAUNCH(ctx, kernel, grid, block, smem, ...)                            \
+    do {                                                                           \
+        kernel<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);           \
+        (ctx)->launches++;                                                         \
+    } while (0)
+
+// Error helpers: set ctx->err and return a status.
+pgd_status pgd_fail(pgd_ctx *ctx, pgd_status s, const std::string &msg);
+pgd_status pgd_cuda_fail(pgd_ctx *ctx, cudaError_t e, const char *what);
+
+#define PGD_CUDA(ctx, call)                                          \
+    do {                                                             \
+        cudaError_t e__ = (call);                                    \
+        if (e__ != cudaSuccess) return pgd_cuda_fail((ctx), e__, #call); \
+    } while (0)
+
+// Device memory owned by a graph (counted against the context budget).
+pgd_status pgd_graph_alloc(pgd_graph *g, void **p, size_t bytes);
+void pgd_graph_free(pgd_graph *g, void *p, size_t bytes);
+
+// Stream-ordered temporaries (not counted against the budget).
+pgd_status pgd_tmp_alloc(pgd_ctx *ctx, void **p, size_t bytes);
+void pgd_tmp_free(pgd_ctx *ctx, void *p);
+
+// Device stages (graph_build.cu).
+pgd_status pgd_build_from_pairs(pgd_graph *g, const int32_t *h_src, const int32_t *h_dst, int64_t k,
+                                int64_t n_min, bool dedup);
+pgd_status pgd_build_from_csr(pgd_graph *g, const int64_t *h_off, const int32_t *h_adj, int64_t n);
+pgd_status pgd_dev_preprocess(pgd_graph *g, int neigh_kind, int s2l);
+pgd_status pgd_dev_cores(pgd_graph *g);
+pgd_status pgd_dev_assortativity(pgd_graph *g, double *r);
+pgd_status pgd_dev_sort_edges(pgd_graph *g, int order_kind, int s2l);
+
+// Decomposition (decompose.cu).
+pgd_status pgd_dev_decompose(pgd_graph *g, bool micro, pgd_counts *out);
+
+// Order kinds shared by host parsing and device keys.
+enum pgd_order_kind {
+    PGD_ORD_NATURAL = 0,
+    PGD_ORD_DEG = 2,
+    PGD_ORD_KCORE = 3,
+    PGD_ORD_KCORE_DEG = 4,
+    PGD_ORD_DEG_VOL = 5,
+    PGD_ORD_KCORE_VOL = 6,
+    PGD_ORD_KCORE_DEG_VOL = 7,
+    PGD_ORD_DEG_U = 99,     // names mapped past VAR: key = degree of e_u
+};
+enum pgd_neigh_kind { PGD_NEIGH_ASREAD = 0, PGD_NEIGH_DEG = 1, PGD_NEIGH_KCORE = 2 };

@@ -59,6 +59,9 @@ def lib():
         L.po_sort_edges.argtypes = [_P, ctypes.c_char_p, ctypes.c_int]
         L.po_decompose.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.po_close.argtypes = [_U64P, ctypes.c_int64, ctypes.c_int64, _U64P]
+        L.po_decompose_sample.restype = ctypes.c_int64
+        L.po_decompose_sample.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int64,
+                                          ctypes.POINTER(ctypes.c_double)]
         for f in ("po_n", "po_m"):
             getattr(L, f).restype = ctypes.c_int64
             getattr(L, f).argtypes = [_P]
@@ -129,6 +132,22 @@ class OracleGraph:
         if L.po_decompose(self.h, int(micro), threads, int(cheap_side)):
             raise RuntimeError("decompose failed")
         return self
+
+    def prepare(self, neigh="deg", s2l_neigh=False, order="deg", s2l=False):
+        """preprocess + cores + sort_edges, no decomposition"""
+        L = lib()
+        if L.po_preprocess(self.h, neigh.encode(), int(s2l_neigh)):
+            raise ValueError("preprocess failed")
+        L.po_compute_cores(self.h)
+        if L.po_sort_edges(self.h, order.encode(), int(s2l)):
+            raise ValueError("sort_edges failed")
+        return self
+
+    def time_sample(self, stride, threads=0, cheap_side=False):
+        """(edges, seconds) of the per-edge loop over every stride-th edge"""
+        sec = ctypes.c_double()
+        k = lib().po_decompose_sample(self.h, threads, int(cheap_side), stride, ctypes.byref(sec))
+        return k, sec.value
 
     def csr(self):
         off = np.zeros(self.n + 1, np.int64)
@@ -212,6 +231,9 @@ def ref_lib():
                                    ctypes.c_int, ctypes.c_char_p]
         R.ref_run.argtypes = [_P, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         R.ref_totals.argtypes = [_P, _U64P]
+        R.ref_run_sample.restype = ctypes.c_longlong
+        R.ref_run_sample.argtypes = [_P, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_longlong,
+                                     ctypes.POINTER(ctypes.c_double)]
         for f in ("ref_n", "ref_m"):
             getattr(R, f).restype = ctypes.c_int64
             getattr(R, f).argtypes = [_P]
@@ -247,6 +269,11 @@ class RefGraph:
     def run(self, order="deg", s2l=False, micro=True, workers=1):
         ref_lib().ref_run(self.h, order.encode(), int(s2l), int(micro), workers)
         return self
+
+    def time_sample(self, stride, order="deg", s2l=False, workers=1):
+        sec = ctypes.c_double()
+        k = ref_lib().ref_run_sample(self.h, order.encode(), int(s2l), workers, stride, ctypes.byref(sec))
+        return k, sec.value
 
     @property
     def n(self):

@@ -1,0 +1,225 @@
+"""The oracle (oracle/pgd_oracle.c) pinned against the reference's golden
+vectors and, where the reference was compiled here, against the reference
+itself.  CPU only."""
+import itertools
+import os
+
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+from helpers import (bign_pairs, brute_force_counts, load_npz, load_toys, mtx_pairs, rows_digest)
+
+SYNTH = ["er250", "rmat12", "ba2000", "er1500"]
+ORDERS = [("deg", False), ("kcore", False), ("natural", False), ("deg", True)]
+
+
+def _rows(g):
+    s, d, c = g.micro()
+    return s, d, c
+
+
+@pytest.mark.parametrize("name", sorted(load_toys().keys()))
+def test_toy_graphs(tmp_path, name):
+    toy = load_toys()[name]
+    p = tmp_path / name
+    p.write_text(toy["text"])
+    g = ol.OracleGraph.from_file(str(p)).run()
+    assert g.n == toy["n"] and g.m == toy["m"] and g.max_core == toy["K"]
+    assert [int(x) for x in g.totals()] == toy["totals"]
+    s, d, c = _rows(g)
+    rows = [[int(a), int(b)] + [int(x) for x in r] for a, b, r in zip(s, d, c)]
+    assert rows == toy["rows"]
+
+
+def test_toy_known_answers(tmp_path):
+    """The counts the reference's toy graphs are built to show."""
+    toys = load_toys()
+    names = ol.TOTAL_NAMES
+    t = dict(zip(names, toys["4-clique.txt"]["totals"]))
+    assert t["total_4_clique"] == 1 and t["total_3_tris"] == 4
+    assert all(t[k] == 0 for k in names if k not in ("total_4_clique", "total_3_tris", "total_2_1edge"))
+    t = dict(zip(names, toys["4-chordal-cycle.txt"]["totals"]))
+    assert t["total_4_chordcycle"] == 1 and t["total_3_tris"] == 2 and t["total_2_star"] == 2
+
+
+def _write_sample_graph(tmp_path, z):
+    p = tmp_path / "sample_graph.csv"
+    with open(p, "w") as f:
+        f.write(str(z["header"]) + "\n")
+        for a, b in z["pairs"]:
+            f.write("%d,%d\n" % (a, b))
+    return str(p)
+
+
+def test_sample_graph_matches_reference_rows(tmp_path):
+    z = load_npz("dd21.npz")
+    path = _write_sample_graph(tmp_path, z)
+    g = ol.OracleGraph.from_file(path).run(order="deg")
+    assert g.n == int(z["n"]) and g.m == int(z["m"]) and g.max_core == int(z["K"])
+    assert (g.totals() == z["totals"]).all()
+    s, d, c = _rows(g)
+    assert (s == z["src"]).all() and (d == z["dst"]).all() and (c == z["cols"]).all()
+    g = ol.OracleGraph.from_file(path).run(order="kcore")
+    s, d, c = _rows(g)
+    assert (g.totals() == z["kc_totals"]).all()
+    assert (s == z["kc_src"]).all() and (d == z["kc_dst"]).all() and (c == z["kc_cols"]).all()
+
+
+def test_sample_graph_golden_columns(tmp_path):
+    """sample_graph.csv ships per-edge counts keyed by its own vertex ids; the
+    reader relabels ids by first appearance (graphlet_core.cpp:424-440)."""
+    z = load_npz("dd21.npz")
+    path = _write_sample_graph(tmp_path, z)
+    g = ol.OracleGraph.from_file(path).run()
+    s, d, c = _rows(g)
+    lookup = {}
+    for a, b in z["pairs"]:
+        if a == b:
+            continue
+        for x in (int(a), int(b)):
+            if x not in lookup:
+                lookup[x] = len(lookup)
+    mine = {}
+    for a, b, r in zip(s - 1, d - 1, c):
+        mine[(min(a, b), max(a, b))] = tuple(int(x) for x in r)
+    assert len(mine) == len(z["pairs"])
+    for (a, b), r in zip(z["pairs"], z["golden_cols"]):
+        ia, ib = lookup[int(a)], lookup[int(b)]
+        assert mine[(min(ia, ib), max(ia, ib))] == tuple(int(x) for x in r)
+
+
+@pytest.mark.parametrize("name", SYNTH)
+def test_synthetic_vs_reference(name):
+    z = load_npz("synth.npz")
+    src, dst = mtx_pairs(z[name + "_u"], z[name + "_v"])
+    for order, s2l in ORDERS:
+        tag = "%s_%s%s" % (name, order, "_s2l" if s2l else "")
+        g = ol.OracleGraph.from_pairs(src, dst).run(order=order, s2l=s2l)
+        n, m, K = z[tag + "_meta"]
+        assert (g.n, g.m, g.max_core) == (n, m, K)
+        assert (g.totals() == z[tag + "_totals"]).all(), tag
+        s, d, c = _rows(g)
+        assert rows_digest(s, d, c) == str(z[tag + "_rows_sha256"]), tag
+
+
+def test_huge_n_wraps_like_reference():
+    z = load_npz("bign.npz")
+    src, dst = bign_pairs(z)
+    g = ol.OracleGraph.from_pairs(src, dst).run(micro=False)
+    assert g.n == int(z["n"]) and g.m == int(z["m"])
+    assert (g.totals() == z["totals"]).all()
+
+
+def _census_ok(n, edges, threads=1):
+    if edges:
+        src = np.array([e[0] for e in edges], np.int32)
+        dst = np.array([e[1] for e in edges], np.int32)
+    else:
+        src = dst = np.zeros(0, np.int32)
+    g = ol.OracleGraph.from_pairs(src, dst, n_min=n).run(micro=False, threads=threads)
+    want = brute_force_counts(n, edges)
+    got = dict(zip(ol.TOTAL_NAMES, (int(x) for x in g.totals())))
+    return got == want, got, want
+
+
+def test_brute_force_all_graphs_on_five_vertices():
+    pairs = list(itertools.combinations(range(5), 2))
+    for mask in range(1 << len(pairs)):
+        edges = [pairs[i] for i in range(len(pairs)) if mask >> i & 1]
+        if not edges:
+            continue
+        ok, got, want = _census_ok(5, edges)
+        assert ok, (edges, got, want)
+
+
+def test_brute_force_random_graphs():
+    rng = np.random.default_rng(11)
+    for trial in range(40):
+        n = int(rng.integers(6, 12))
+        p = float(rng.uniform(0.1, 0.9))
+        edges = [(i, j) for i in range(n) for j in range(i + 1, n) if rng.random() < p]
+        if not edges:
+            continue
+        ok, got, want = _census_ok(n, edges)
+        assert ok, (n, edges, got, want)
+
+
+def test_closing_identities_hold():
+    """graphlet_core.cpp:1275-1305 checks these relations between the totals
+    and the raw sums (dead code in the reference; used here as a check)."""
+    z = load_npz("synth.npz")
+    src, dst = mtx_pairs(z["rmat12_u"], z["rmat12_v"])
+    g = ol.OracleGraph.from_pairs(src, dst).run(micro=False)
+    t = dict(zip(ol.TOTAL_NAMES, (int(x) for x in g.totals())))
+    s = [int(x) for x in g.sums()]
+    N = {i: s[4 + i] for i in range(1, 11)}
+    M = (1 << 64) - 1
+    assert (t["total_4_chordcycle"] + 6 * t["total_4_clique"]) & M == N[3]
+    assert (t["total_4_path"] + 4 * t["total_4_cycle"]) & M == N[5]
+    assert (3 * t["total_3_star"] + t["total_4_tailed_tris"]) & M == N[6]
+    assert (2 * t["total_4_tailed_tris"] + 4 * t["total_4_chordcycle"]) & M == N[4]
+    assert (2 * t["total_4_2edge"] + t["total_4_1edge"]) & M == N[8]
+
+
+# ---------------------------------------------------------------------------
+# live reference (only where it was compiled: oracle/_ref)
+
+needs_ref = pytest.mark.skipif(not ol.ref_available(), reason="reference not compiled here")
+
+EDGE_LIST_CASES = {
+    "a.csv": "1,2\n2,3\n3,1\n3,4\n4,5\n5,3\n1,2\n2,2\n",
+    "b.txt": "% comment\n1 2\n2 3\n3 1\n3 4\n4 1\n7 8\n8 3\n",
+    "c.edges": "0 1\n1 2\n2 0\n2 3\n3 0\n1 3\n",
+    "d.tab": "5\t9\n9\t11\n11\t5\n5\t2\n2\t9\n",
+    "e.csv": "src,dst,w\n10,20,1\n20,30,1\n30,10,1\n10,40,2\n",
+    "f.txt": "# header\n1 2 0.5\n2 3 0.5\n1 3 0.5\n3 4 1.0\n4 5 1\n5 1 1\n",
+}
+
+
+@needs_ref
+@pytest.mark.parametrize("fname", sorted(EDGE_LIST_CASES))
+def test_reader_rules_vs_reference(tmp_path, fname):
+    p = tmp_path / fname
+    p.write_text(EDGE_LIST_CASES[fname])
+    r = ol.RefGraph.from_file(str(p)).run(micro=True)
+    g = ol.OracleGraph.from_file(str(p)).run(micro=True)
+    assert (g.n, g.m) == (r.n, r.m)
+    assert (g.totals() == r.totals()).all()
+    a, b, c = g.micro()
+    x, y, z = r.micro()
+    assert (a == x).all() and (b == y).all() and (c == z).all()
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", range(6))
+def test_random_graphs_vs_reference(seed):
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(30, 200))
+    k = int(rng.integers(n, 6 * n))
+    src = rng.integers(0, n, k).astype(np.int32)
+    dst = rng.integers(0, n, k).astype(np.int32)
+    g = ol.OracleGraph.from_pairs(src, dst, dedup=True)
+    off, adj = g.csr()
+    order = ["deg", "kcore", "natural", "kcore_deg", "deg_vol", "triangles"][seed]
+    r = ol.RefGraph.from_csr(off, adj).run(order=order, micro=True)
+    o = ol.OracleGraph.from_csr(off, adj).run(order=order, micro=True)
+    assert (o.totals() == r.totals()).all()
+    a, b, c = o.micro()
+    x, y, z = r.micro()
+    assert (a == x).all() and (b == y).all() and (c == z).all()
+    assert o.max_core == r.max_core
+
+
+@needs_ref
+@pytest.mark.parametrize("neigh,s2l", [("kcore", False), ("natural", False), ("deg", True)])
+def test_neighbour_orders_vs_reference(neigh, s2l):
+    z = load_npz("synth.npz")
+    src, dst = mtx_pairs(z["ba2000_u"], z["ba2000_v"])
+    g = ol.OracleGraph.from_pairs(src, dst)
+    off, adj = g.csr()
+    r = ol.RefGraph.from_csr(off, adj, neigh=neigh, s2l_neigh=s2l).run(micro=True)
+    o = ol.OracleGraph.from_csr(off, adj).run(neigh=neigh, s2l_neigh=s2l, micro=True)
+    a, b, c = o.micro()
+    x, y, w = r.micro()
+    assert (a == x).all() and (b == y).all() and (c == w).all()
