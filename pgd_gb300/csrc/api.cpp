@@ -54,6 +54,14 @@ void pgd_tmp_free(pgd_ctx *ctx, void *p) {
     if (p) cudaFreeAsync(p, ctx->stream);
 }
 
+// Copies on the context's stream and waits for it: the stream is created
+// non-blocking, so a legacy-stream cudaMemcpy would not wait for its kernels.
+static cudaError_t pgd_copy_sync(pgd_ctx *ctx, void *dst, const void *src, size_t bytes, cudaMemcpyKind kind) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, ctx->stream);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(ctx->stream);
+}
+
 // ---------------------------------------------------------------------------
 // context
 
@@ -152,6 +160,10 @@ extern "C" pgd_status pgd_graph_destroy(pgd_graph *g) {
     pgd_graph_free(g, g->core, (g->n + 1) * sizeof(int32_t));
     pgd_graph_free(g, g->order, (g->m + 1) * sizeof(int32_t));
     pgd_graph_free(g, g->micro, (g->m + 1) * PGD_NMICRO * sizeof(uint64_t));
+    pgd_graph_free(g, g->offp, (g->n + 1) * sizeof(int64_t));
+    pgd_graph_free(g, g->adjp, (g->m + 1) * sizeof(int32_t));
+    pgd_graph_free(g, g->hubid, (g->n + 1) * sizeof(int32_t));
+    pgd_graph_free(g, g->tslot, (2 * g->m + 1) * sizeof(uint32_t));
     // whatever is left (partial builds) is returned to the budget as well
     g->ctx->resident -= g->bytes;
     cudaStreamSynchronize(g->ctx->stream);
@@ -270,7 +282,7 @@ extern "C" pgd_status pgd_get_kcore(pgd_graph *g, int32_t *kcore) {
     pgd_status st = pgd_compute_cores(g, nullptr);
     if (st) return st;
     kcore[0] = 0;
-    if (g->n) PGD_CUDA(g->ctx, cudaMemcpy(kcore + 1, g->core, g->n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (g->n) PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, kcore + 1, g->core, g->n * sizeof(int32_t), cudaMemcpyDeviceToHost));
     return PGD_OK;
 }
 
@@ -334,16 +346,16 @@ extern "C" pgd_status pgd_get_edges(pgd_graph *g, int64_t *ev, int64_t *eu, int3
     cudaSetDevice(g->ctx->device);
     std::vector<int32_t> tmp((size_t)g->m + 1);
     if (ev) {
-        PGD_CUDA(g->ctx, cudaMemcpy(tmp.data(), g->ev, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, tmp.data(), g->ev, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
         for (int64_t i = 0; i < g->m; i++) ev[i] = tmp[i];
     }
     if (eu) {
-        PGD_CUDA(g->ctx, cudaMemcpy(tmp.data(), g->eu, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, tmp.data(), g->eu, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
         for (int64_t i = 0; i < g->m; i++) eu[i] = tmp[i];
     }
     if (order) {
         if (!g->sorted) return pgd_fail(g->ctx, PGD_EINVAL, "edges are not sorted");
-        PGD_CUDA(g->ctx, cudaMemcpy(order, g->order, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, order, g->order, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
     }
     return PGD_OK;
 }
@@ -353,13 +365,13 @@ extern "C" pgd_status pgd_get_micro(pgd_graph *g, int64_t *src1, int64_t *dst1, 
     if (!g->has_micro) return pgd_fail(g->ctx, PGD_EINVAL, "no per-edge results: decompose with PGD_MICRO first");
     cudaSetDevice(g->ctx->device);
     if (cols && g->m)
-        PGD_CUDA(g->ctx, cudaMemcpy(cols, g->micro, g->m * PGD_NMICRO * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+        PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, cols, g->micro, g->m * PGD_NMICRO * sizeof(uint64_t), cudaMemcpyDeviceToHost));
     if (src1 || dst1) {
         std::vector<int32_t> ev((size_t)g->m + 1), eu((size_t)g->m + 1), ord((size_t)g->m + 1);
         if (g->m) {
-            PGD_CUDA(g->ctx, cudaMemcpy(ev.data(), g->ev, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
-            PGD_CUDA(g->ctx, cudaMemcpy(eu.data(), g->eu, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
-            PGD_CUDA(g->ctx, cudaMemcpy(ord.data(), g->order, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
+            PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, ev.data(), g->ev, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
+            PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, eu.data(), g->eu, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
+            PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, ord.data(), g->order, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
         }
         for (int64_t e = 0; e < g->m; e++) {
             if (src1) src1[e] = (int64_t)ev[ord[e]] + 1;

@@ -53,6 +53,14 @@ struct pgd_graph {
     // per-edge results in E_ordered order
     bool has_micro = false;
     uint64_t *micro = nullptr;        // m * 8
+
+    // decomposition structures, built on first use (decompose.cu)
+    bool has_aux = false;
+    int64_t *offp = nullptr;          // n+1: degree-oriented lists N+(x)
+    int32_t *adjp = nullptr;          // m: neighbours of higher (degree, id)
+    int32_t *hubid = nullptr;         // n: slot in the W cache, -1 if none
+    int32_t nhubs = 0;
+    uint32_t *tslot = nullptr;        // 2m: triangle count of each slot's edge
 };
 
 // Launch one of this library's kernels on the context's stream and count it.
