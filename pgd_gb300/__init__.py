@@ -45,7 +45,7 @@ EXPORTS = [
     "pgd_preprocess", "pgd_compute_cores", "pgd_get_kcore", "pgd_assortativity",
     "pgd_sort_edges", "pgd_decompose", "pgd_get_micro", "pgd_get_edges", "pgd_close_counts",
     "pgd_decompose_batch", "pgd_gen_u01", "pgd_gen_rmat", "pgd_gen_er", "pgd_gen_ba",
-    "pgd_gen_rgg3d",
+    "pgd_gen_rgg3d", "pgd_decompose_csr_noalloc", "pgd_noalloc_scratch_bytes",
 ]
 
 
@@ -123,6 +123,10 @@ def lib():
                                             ctypes.c_int64]),
             "pgd_gen_rgg3d": (ctypes.c_int64, [ctypes.c_int64, ctypes.c_double, ctypes.c_uint64, _I32,
                                                _I32, ctypes.c_int64]),
+            "pgd_decompose_csr_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+                                                         _P, ctypes.POINTER(pgd_counts), ctypes.c_char_p,
+                                                         ctypes.c_size_t]),
+            "pgd_noalloc_scratch_bytes": (ctypes.c_uint64, []),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

@@ -37,7 +37,11 @@
 // are reproduced with explicitly rounded double intrinsics.  Partial sums
 // are uint64 and wrap exactly like the reference's (addition mod 2^64 is
 // order independent, so the reduction order does not matter).
+#include <string.h>
+
 #include <cub/cub.cuh>
+#include <mutex>
+#include <string>
 
 #include "pgd_internal.h"
 #include "pgd_kernels.cuh"
@@ -783,5 +787,278 @@ pgd_status pgd_dev_decompose(pgd_graph *g, bool micro, pgd_counts *out) {
     out->kernel_ms = ms;
     pgd_close_counts(out->sums, g->n, g->m, out->totals);
     g->has_micro = micro;
+    return PGD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free decomposition (no counterpart in the reference).
+//
+// Some callers cannot allocate device memory at the moment they need counts:
+// code inside a framework that hands out a fixed workspace and forbids
+// allocation (inference plugins, custom ops), code recorded into a CUDA
+// stream capture where cudaMalloc is not permitted, and latency-critical
+// loops where cudaMalloc/cudaFree would synchronise the device.  For them
+// pgd_decompose_csr_noalloc runs the same kernels on a caller's device CSR
+// with every intermediate carved out of one file-scope device array of
+// kNoAllocScratchBytes, and it never calls cudaMalloc, cudaFree or an
+// allocating library routine.
+//
+// The array is a __device__ object: every GPU that loads this library holds
+// kNoAllocScratchBytes for it until the process exits.  All calls share it,
+// and each call clears what must start at zero; calls that overlap on the
+// GPU (two streams, two threads) race on it and must be serialised by the
+// caller.  Host code must not use the array's name as an address: its
+// device address is looked up with cudaGetSymbolAddress once per device, by
+// the first call on that device, so that first call should come before any
+// stream capture.
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 64ull << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Rows must be sorted, in range, free of self loops, and symmetric.
+__global__ void k_na_check(const int64_t *off, const int32_t *adj, const int32_t *row, int64_t n, int64_t nnz,
+                           unsigned long long *bad) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nnz; j += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t r = row[j], c = adj[j];
+        bool ok = c >= 0 && c < n && c != r && (j == off[r] || adj[j - 1] < c);
+        if (ok) ok = pgd_contains(adj + off[c], (int)(off[c + 1] - off[c]), r);
+        if (!ok) atomicAdd(bad, 1ull);
+    }
+}
+
+__global__ void k_na_degrees(const int64_t *off, int64_t n, int32_t *deg) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        deg[v] = (int32_t)(off[v + 1] - off[v]);
+}
+
+__global__ void k_na_edge_flags(const int32_t *row, const int32_t *adj, int64_t nnz, uint32_t *flag) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nnz; j += (int64_t)gridDim.x * blockDim.x)
+        flag[j] = row[j] < adj[j] ? 1u : 0u;
+}
+
+__global__ void k_na_edges(const int32_t *row, const int32_t *adj, const uint32_t *flag, const uint32_t *pos,
+                           int64_t nnz, int32_t *ev, int32_t *eu, int32_t *order) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nnz; j += (int64_t)gridDim.x * blockDim.x) {
+        if (!flag[j]) continue;
+        const uint32_t id = pos[j];
+        ev[id] = row[j];
+        eu[id] = adj[j];
+        order[id] = (int32_t)id;
+    }
+}
+
+// Bump allocator over the scratch array (host-side bookkeeping only).
+struct Carve {
+    unsigned char *base;
+    size_t used = 0, limit;
+    bool ok = true;
+    template <typename T>
+    T *take(size_t count) {
+        size_t bytes = ((count * sizeof(T)) + 255) & ~(size_t)255;
+        if (used + bytes > limit) { ok = false; return nullptr; }
+        T *p = (T *)(base + used);
+        used += bytes;
+        return p;
+    }
+};
+
+void na_msg(char *err, size_t errlen, const std::string &m) {
+    if (err && errlen) {
+        size_t k = std::min(errlen - 1, m.size());
+        memcpy(err, m.data(), k);
+        err[k] = 0;
+    }
+}
+
+}  // namespace
+
+#define NA_CUDA(call)                                                                         \
+    do {                                                                                      \
+        cudaError_t e__ = (call);                                                             \
+        if (e__ != cudaSuccess) {                                                             \
+            na_msg(err, errlen, std::string("CUDA error ") + cudaGetErrorString(e__) + " in " #call); \
+            return e__ == cudaErrorMemoryAllocation ? PGD_ENOMEM : PGD_ECUDA;                  \
+        }                                                                                     \
+    } while (0)
+
+extern "C" uint64_t pgd_noalloc_scratch_bytes(void) { return kNoAllocScratchBytes; }
+
+extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int32_t *d_adj, int64_t n, int64_t nnz,
+                                                int device, void *stream_, pgd_counts *out, char *err,
+                                                size_t errlen) {
+    if (!d_off || (nnz > 0 && !d_adj) || n < 0 || nnz < 0 || (nnz & 1) || !out) {
+        na_msg(err, errlen, "bad arguments (device CSR pointers, n >= 0, even nnz, out)");
+        return PGD_EINVAL;
+    }
+    if (device < 0 || device >= kNoAllocMaxDevices || n > 0x7ffffffe || nnz > 0x7fffffff) {
+        na_msg(err, errlen, "device ordinal or graph size out of range");
+        return PGD_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream_;
+    NA_CUDA(cudaSetDevice(device));
+    unsigned char *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_addr[device]) {
+            void *ptr = nullptr;
+            NA_CUDA(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+            g_noalloc_addr[device] = (unsigned char *)ptr;
+        }
+        base = g_noalloc_addr[device];
+    }
+    int nsm = 0;
+    NA_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+    const int64_t m = nnz / 2;
+    const int64_t nwords = (n + 31) / 32;
+    const bool in_smem = nwords * 4 <= kMaxSmemBitmap;
+    const int64_t hub_bound = std::max<int64_t>(1, std::min<int64_t>(n, nnz / kCacheHub + 1));
+
+    // CUB temporary storage sizes (queries only)
+    size_t tb_scan = 0, tb_sort = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tb_scan, (uint32_t *)nullptr, (uint32_t *)nullptr, std::max(nnz, n) + 1, s);
+    cub::DeviceRadixSort::SortKeys(nullptr, tb_sort, (uint64_t *)nullptr, (uint64_t *)nullptr, std::max<int64_t>(m, 1),
+                                   0, 64, s);
+
+    // carve every buffer up front, with upper bounds, so an oversized graph
+    // is refused before anything runs
+    Carve C{base, 0, kNoAllocScratchBytes};
+    unsigned long long *sums = C.take<unsigned long long>(PGD_NSUMS + 1);
+    unsigned long long *ctr = C.take<unsigned long long>(8);
+    int32_t *deg = C.take<int32_t>(n + 1);
+    int32_t *row = C.take<int32_t>(nnz + 1);
+    uint32_t *flag = C.take<uint32_t>(std::max(nnz, n) + 2);
+    uint32_t *pos = C.take<uint32_t>(std::max(nnz, n) + 2);
+    int32_t *ev = C.take<int32_t>(m + 1);
+    int32_t *eu = C.take<int32_t>(m + 1);
+    int32_t *order = C.take<int32_t>(m + 1);
+    int64_t *offp = C.take<int64_t>(n + 1);
+    int32_t *adjp = C.take<int32_t>(m + 1);
+    int32_t *hubid = C.take<int32_t>(n + 1);
+    uint32_t *tslot = C.take<uint32_t>(nnz + 1);
+    uint64_t *keys = C.take<uint64_t>(m + 1);
+    uint64_t *keys2 = C.take<uint64_t>(m + 1);
+    int32_t *posv = C.take<int32_t>(m + 1);
+    uint32_t *iflag = C.take<uint32_t>(m + 2);
+    uint32_t *ipos = C.take<uint32_t>(m + 2);
+    int64_t *items = C.take<int64_t>(m + 2);
+    unsigned long long *cache = C.take<unsigned long long>((size_t)nsm * hub_bound);
+    uint32_t *gbm = in_smem ? nullptr : C.take<uint32_t>((size_t)nsm * nwords);
+    void *tmp = C.take<unsigned char>(std::max(tb_scan, tb_sort) + 16);
+    if (!C.ok) {
+        na_msg(err, errlen, "graph too large for the allocation-free path: needs more than the " +
+                                std::to_string(kNoAllocScratchBytes >> 20) + " MiB scratch array (n=" +
+                                std::to_string(n) + ", nnz=" + std::to_string(nnz) + ")");
+        return PGD_ENOMEM;
+    }
+    size_t tb = std::max(tb_scan, tb_sort) + 16;
+
+    NA_CUDA(cudaMemsetAsync(sums, 0, (PGD_NSUMS + 1) * sizeof(unsigned long long), s));
+    NA_CUDA(cudaMemsetAsync(ctr, 0, 8 * sizeof(unsigned long long), s));
+    memset(out, 0, sizeof(*out));
+    out->n = n;
+    out->m = m;
+    if (m == 0) {
+        pgd_close_counts(out->sums, n, m, out->totals);
+        return PGD_OK;
+    }
+    // validate and derive the per-graph structures
+    k_rows<<<grid_for(nnz), kThreads, 0, s>>>(d_off, n, nnz, row);
+    k_na_check<<<grid_for(nnz), kThreads, 0, s>>>(d_off, d_adj, row, n, nnz, ctr + 3);
+    k_na_degrees<<<grid_for(n), kThreads, 0, s>>>(d_off, n, deg);
+    unsigned long long bad = 0;
+    NA_CUDA(cudaMemcpyAsync(&bad, ctr + 3, sizeof(bad), cudaMemcpyDeviceToHost, s));
+    NA_CUDA(cudaStreamSynchronize(s));
+    if (bad) {
+        na_msg(err, errlen, "device CSR rejected: rows must be sorted, symmetric, in range and free of self loops");
+        return PGD_EINVAL;
+    }
+    k_na_edge_flags<<<grid_for(nnz), kThreads, 0, s>>>(row, d_adj, nnz, flag);
+    NA_CUDA(cudaMemsetAsync(flag + nnz, 0, sizeof(uint32_t), s));
+    NA_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, nnz + 1, s));
+    k_na_edges<<<grid_for(nnz), kThreads, 0, s>>>(row, d_adj, flag, pos, nnz, ev, eu, order);
+    k_oriented_flags<<<grid_for(nnz), kThreads, 0, s>>>(row, d_adj, deg, nnz, flag);
+    NA_CUDA(cudaMemsetAsync(flag + nnz, 0, sizeof(uint32_t), s));
+    NA_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, nnz + 1, s));
+    k_oriented_fill<<<grid_for(std::max(nnz, n + 1)), kThreads, 0, s>>>(d_off, d_adj, flag, pos, n, nnz, offp, adjp);
+    k_hub_flags<<<grid_for(n), kThreads, 0, s>>>(deg, n, flag);
+    NA_CUDA(cudaMemsetAsync(flag + n, 0, sizeof(uint32_t), s));
+    NA_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, n + 1, s));
+    k_hub_ids<<<grid_for(n), kThreads, 0, s>>>(flag, pos, n, hubid);
+
+    DevGraph G;
+    G.off = d_off;
+    G.adj = d_adj;
+    G.deg = deg;
+    G.offp = offp;
+    G.adjp = adjp;
+    G.hubid = hubid;
+    G.tslot = tslot;
+    G.ev = ev;
+    G.eu = eu;
+    G.order = order;
+    G.n = n;
+    G.m = m;
+    G.micro = nullptr;
+    G.sums = sums;
+    k_tslot<<<grid_for(32 * m), kThreads, 0, s>>>(G, tslot);
+    k_plan_keys<<<grid_for(m), kThreads, 0, s>>>(G, keys, ctr);
+    NA_CUDA(cub::DeviceRadixSort::SortKeys(tmp, tb, keys, keys2, m, 0, 64, s));
+    k_keys_pos<<<grid_for(m), kThreads, 0, s>>>(keys2, m, posv);
+    unsigned long long nh = 0;
+    uint32_t nhubs = 0;
+    NA_CUDA(cudaMemcpyAsync(&nh, ctr, sizeof(nh), cudaMemcpyDeviceToHost, s));
+    NA_CUDA(cudaMemcpyAsync(&nhubs, pos + n, sizeof(nhubs), cudaMemcpyDeviceToHost, s));
+    NA_CUDA(cudaStreamSynchronize(s));
+    int64_t nitems = 0;
+    if (nh > 0) {
+        k_item_flags<<<grid_for(nh), kThreads, 0, s>>>(keys2, (int64_t)nh, iflag);
+        NA_CUDA(cudaMemsetAsync(iflag + nh, 0, sizeof(uint32_t), s));
+        NA_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, iflag, ipos, (int64_t)nh + 1, s));
+        uint32_t ni = 0;
+        NA_CUDA(cudaMemcpyAsync(&ni, ipos + nh, sizeof(ni), cudaMemcpyDeviceToHost, s));
+        NA_CUDA(cudaStreamSynchronize(s));
+        nitems = ni;
+        k_item_fill<<<grid_for(nh), kThreads, 0, s>>>(iflag, ipos, (int64_t)nh, items);
+    }
+    if (nitems > 0) {
+        const int nh_slots = std::max(1, (int)nhubs);
+        NA_CUDA(cudaMemsetAsync(cache, 0xff, (size_t)nsm * nh_slots * sizeof(unsigned long long), s));
+        if (!in_smem) NA_CUDA(cudaMemsetAsync(gbm, 0, (size_t)nsm * nwords * 4, s));
+        const size_t smem = in_smem ? (size_t)nwords * 4 : 0;
+        NA_CUDA(cudaFuncSetAttribute(k_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        HubArgs H;
+        H.G = G;
+        H.hpos = posv;
+        H.items = items;
+        H.nitems = nitems;
+        H.cache = cache;
+        H.nhubs = nh_slots;
+        H.gbitmap = gbm;
+        H.nwords = nwords;
+        H.smem_bitmap = in_smem ? 1 : 0;
+        H.next = ctr + 1;
+        k_hub<<<nsm, kHubWarps * 32, smem, s>>>(H);
+    }
+    const int64_t nlight = m - (int64_t)nh;
+    if (nlight > 0) {
+        LightArgs L;
+        L.G = G;
+        L.lpos = posv + nh;
+        L.nlight = nlight;
+        L.next = ctr + 2;
+        k_light<<<nsm * 8, kLightWarps * 32, 0, s>>>(L);
+    }
+    NA_CUDA(cudaGetLastError());
+    unsigned long long h[PGD_NSUMS];
+    NA_CUDA(cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, s));
+    NA_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < PGD_NSUMS; i++) out->sums[i] = h[i];
+    pgd_close_counts(out->sums, n, m, out->totals);
     return PGD_OK;
 }
