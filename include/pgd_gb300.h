@@ -192,12 +192,78 @@ void pgd_close_counts(const uint64_t sums[PGD_NSUMS], int64_t n, int64_t m,
                       uint64_t totals[PGD_NTOTALS]);
 
 /* ---- batched decomposition (no reference counterpart) ------------------
- * Many independent graphs in one persistent launch over a device work queue
- * of (graph, edge-span) items; per-graph results identical to
- * pgd_decompose.  Graphs must be preprocessed and sorted (or are, with
- * "deg" defaults).  out has k entries. */
+ * Many independent graphs decomposed together: the batch becomes one
+ * disjoint-union graph on the device and runs through the same persistent
+ * work-queue kernels (work items are (anchor, edge chunk) and edge spans of
+ * every graph); per-graph results are identical to pgd_decompose (closed
+ * forms use each graph's own n and m, sums are kept per graph).  Graphs not
+ * yet preprocessed/sorted get the "deg" defaults.  With PGD_MICRO each
+ * graph's per-edge rows are written to that graph (read with
+ * pgd_get_micro).  out has k entries; kernel_ms is the batch's. */
 pgd_status pgd_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k, uint32_t flags,
                                pgd_counts *out);
+
+/* Batched decomposition straight from host pair lists (no reference
+ * counterpart): graph g is the pairs [pair_off[g], pair_off[g+1]) of
+ * src/dst (0-based ids local to the graph; edge-list rules: symmetrised,
+ * deduplicated, self loops dropped), with n = max(n_min[g], 1 + largest id
+ * with an edge) (n_min may be NULL).  The whole batch is built as one device
+ * CSR and decomposed in one pass; out[g] gets graph g's global counts,
+ * identical to building and decomposing it alone. */
+pgd_status pgd_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pair_off, const int32_t *src,
+                                     const int32_t *dst, const int64_t *n_min, pgd_counts *out);
+
+/* ---- request server (no reference counterpart) ---------------------------
+ * Continuous batching: submitted graphs queue; `workers` threads, each with
+ * its own context and stream, repeatedly admit the oldest pending requests
+ * that fit the HBM budget (at most max_batch), decompose them together with
+ * pgd_decompose_pairs_batch, and publish each request's global counts.
+ * Requests that arrive while a batch runs join the next one; batches of
+ * different workers run on the device at the same time.  A request whose own
+ * memory estimate exceeds the budget completes with PGD_ENOMEM. */
+typedef struct pgd_server pgd_server;
+typedef struct {
+    int device;
+    int workers;           /* default 2                                     */
+    int max_batch;         /* requests per batch, default 4096              */
+    int reserved;
+    uint64_t hbm_budget;   /* bytes of admitted work; 0 = half of the device's free memory */
+} pgd_server_opts;
+typedef struct {
+    uint64_t submitted, completed, rejected, batches;
+    uint64_t inflight_bytes, peak_bytes;
+    double p50_ms, p99_ms, mean_ms;   /* submit -> result latency            */
+    double graphs_per_s;              /* completed / (last completion - first submit) */
+} pgd_server_stat;
+pgd_status pgd_server_create(const pgd_server_opts *opts, pgd_server **out);
+pgd_status pgd_server_submit(pgd_server *sv, const int32_t *src, const int32_t *dst, int64_t k, int64_t n_min,
+                             uint64_t *ticket);
+/* *done = 1 when finished: out gets the counts, the ticket is released and
+ * the request's own status is returned. */
+pgd_status pgd_server_poll(pgd_server *sv, uint64_t ticket, pgd_counts *out, int *done);
+/* Waits up to timeout_ms; PGD_ETIMEOUT if the request is still running. */
+pgd_status pgd_server_wait(pgd_server *sv, uint64_t ticket, int timeout_ms, pgd_counts *out);
+pgd_status pgd_server_stats(pgd_server *sv, pgd_server_stat *st);
+/* Finishes the queued requests, then stops the workers. */
+pgd_status pgd_server_destroy(pgd_server *sv);
+
+/* ---- thresholds and autotuning (no reference counterpart) --------------
+ * Three thresholds steer how the decomposition kernels split work; counts
+ * never depend on them.  anchor_hub (2..256, default 128): anchors of degree
+ * >= it are processed one CTA per anchor with N(p) as a bitmap, below it one
+ * warp per edge with N(p) staged and searched.  cache_hub (>= 2, default
+ * 64): W(w,p) is cached per anchor for neighbours of degree >= it, below it
+ * N(w) is scanned per edge.  dense_max (0..2048, default 2048): in a batch,
+ * graphs of at most this many vertices are decomposed with whole adjacency
+ * rows as bitsets (one 2048-bit row per warp), larger ones with sorted
+ * lists.  pgd_autotune decomposes the given graphs `reps` times per
+ * candidate -- first dense_max in {0, 256, 1024, 2048}, then 16
+ * (anchor_hub, cache_hub) pairs -- checks that every candidate gives
+ * identical counts, keeps the fastest on the context and reports it. */
+pgd_status pgd_set_thresholds(pgd_ctx *ctx, int anchor_hub, int cache_hub, int dense_max);
+pgd_status pgd_get_thresholds(const pgd_ctx *ctx, int *anchor_hub, int *cache_hub, int *dense_max);
+pgd_status pgd_autotune(pgd_ctx *ctx, pgd_graph *const *graphs, int k, int reps, int *anchor_hub, int *cache_hub,
+                        int *dense_max, float *best_ms);
 
 /* ---- allocation-free decomposition --------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

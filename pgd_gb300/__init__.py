@@ -45,7 +45,9 @@ EXPORTS = [
     "pgd_preprocess", "pgd_compute_cores", "pgd_get_kcore", "pgd_assortativity",
     "pgd_sort_edges", "pgd_decompose", "pgd_get_micro", "pgd_get_edges", "pgd_close_counts",
     "pgd_decompose_batch", "pgd_gen_u01", "pgd_gen_rmat", "pgd_gen_er", "pgd_gen_ba",
-    "pgd_gen_rgg3d", "pgd_decompose_csr_noalloc", "pgd_noalloc_scratch_bytes",
+    "pgd_gen_rgg3d", "pgd_decompose_csr_noalloc", "pgd_noalloc_scratch_bytes", "pgd_set_thresholds",
+    "pgd_get_thresholds", "pgd_autotune", "pgd_decompose_pairs_batch", "pgd_server_create", "pgd_server_submit",
+    "pgd_server_poll", "pgd_server_wait", "pgd_server_stats", "pgd_server_destroy",
 ]
 
 
@@ -64,6 +66,18 @@ class pgd_counts(ctypes.Structure):
     _fields_ = [("totals", ctypes.c_uint64 * NTOTALS), ("sums", ctypes.c_uint64 * NSUMS),
                 ("n", ctypes.c_int64), ("m", ctypes.c_int64), ("kernel_ms", ctypes.c_float),
                 ("reserved", ctypes.c_float * 3)]
+
+
+class pgd_server_opts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("workers", ctypes.c_int), ("max_batch", ctypes.c_int),
+                ("reserved", ctypes.c_int), ("hbm_budget", ctypes.c_uint64)]
+
+
+class pgd_server_stat(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("rejected", ctypes.c_uint64),
+                ("batches", ctypes.c_uint64), ("inflight_bytes", ctypes.c_uint64), ("peak_bytes", ctypes.c_uint64),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
+                ("graphs_per_s", ctypes.c_double)]
 
 
 class pgd_info(ctypes.Structure):
@@ -127,6 +141,22 @@ def lib():
                                                          _P, ctypes.POINTER(pgd_counts), ctypes.c_char_p,
                                                          ctypes.c_size_t]),
             "pgd_noalloc_scratch_bytes": (ctypes.c_uint64, []),
+            "pgd_set_thresholds": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+            "pgd_decompose_pairs_batch": (ctypes.c_int, [_P, ctypes.c_int, _I64, _I32, _I32, _P,
+                                                         ctypes.POINTER(pgd_counts)]),
+            "pgd_server_create": (ctypes.c_int, [ctypes.POINTER(pgd_server_opts), _PP]),
+            "pgd_server_submit": (ctypes.c_int, [_P, _I32, _I32, ctypes.c_int64, ctypes.c_int64,
+                                                 ctypes.POINTER(ctypes.c_uint64)]),
+            "pgd_server_poll": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.POINTER(pgd_counts),
+                                               ctypes.POINTER(ctypes.c_int)]),
+            "pgd_server_wait": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(pgd_counts)]),
+            "pgd_server_stats": (ctypes.c_int, [_P, ctypes.POINTER(pgd_server_stat)]),
+            "pgd_server_destroy": (ctypes.c_int, [_P]),
+            "pgd_get_thresholds": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                                  ctypes.POINTER(ctypes.c_int)]),
+            "pgd_autotune": (ctypes.c_int, [_P, _PP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_float)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -218,6 +248,38 @@ class Context:
                     "pgd_graph_from_file")
         return Graph(self, h)
 
+    def set_thresholds(self, anchor_hub, cache_hub, dense_max=2048):
+        self._check(lib().pgd_set_thresholds(self.h, anchor_hub, cache_hub, dense_max), "pgd_set_thresholds")
+
+    def thresholds(self):
+        a, c, d = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._check(lib().pgd_get_thresholds(self.h, ctypes.byref(a), ctypes.byref(c), ctypes.byref(d)),
+                    "pgd_get_thresholds")
+        return a.value, c.value, d.value
+
+    def autotune(self, graphs, reps=1):
+        """Pick the fastest thresholds for these graphs; returns (anchor_hub, cache_hub, dense_max, ms)."""
+        arr = (ctypes.c_void_p * len(graphs))(*[g.h.value for g in graphs])
+        a, c, d, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        self._check(lib().pgd_autotune(self.h, arr, len(graphs), reps, ctypes.byref(a), ctypes.byref(c),
+                                       ctypes.byref(d), ctypes.byref(ms)), "pgd_autotune")
+        return a.value, c.value, d.value, ms.value
+
+    def decompose_pairs_batch(self, graphs, n_min=None):
+        """graphs: list of (src, dst) local-id pair arrays.  One device build and one pass for all."""
+        off = np.zeros(len(graphs) + 1, np.int64)
+        for i, (s, _) in enumerate(graphs):
+            off[i + 1] = off[i] + len(s)
+        src = np.ascontiguousarray(np.concatenate([s for s, _ in graphs]) if graphs else np.zeros(1), np.int32)
+        dst = np.ascontiguousarray(np.concatenate([d for _, d in graphs]) if graphs else np.zeros(1), np.int32)
+        if len(src) == 0:
+            src = dst = np.zeros(1, np.int32)
+        nm = None if n_min is None else np.ascontiguousarray(n_min, np.int64)
+        out = (pgd_counts * len(graphs))()
+        self._check(lib().pgd_decompose_pairs_batch(self.h, len(graphs), off, src, dst, _ptr(nm), out),
+                    "pgd_decompose_pairs_batch")
+        return [Counts(c) for c in out]
+
     def decompose_batch(self, graphs, micro=False):
         arr = (ctypes.c_void_p * len(graphs))(*[g.h.value for g in graphs])
         out = (pgd_counts * len(graphs))()
@@ -307,6 +369,61 @@ class Graph:
         order = np.empty(max(m, 1), np.int32) if with_order else None
         self.ctx._check(lib().pgd_get_edges(self.h, _ptr(ev), _ptr(eu), _ptr(order)), "pgd_get_edges")
         return ev[:m], eu[:m], (order[:m] if with_order else None)
+
+
+class Server:
+    """Continuous-batching request server (pgd_server_*)."""
+
+    def __init__(self, device=0, workers=2, max_batch=4096, hbm_budget=0):
+        o = pgd_server_opts(device, workers, max_batch, 0, hbm_budget)
+        h = ctypes.c_void_p()
+        st = lib().pgd_server_create(ctypes.byref(o), ctypes.byref(h))
+        if st:
+            raise PGDError(st, "pgd_server_create failed")
+        self.h = h
+
+    def submit(self, src, dst, n_min=0):
+        src = np.ascontiguousarray(src, np.int32)
+        dst = np.ascontiguousarray(dst, np.int32)
+        if len(src) == 0:
+            src = dst = np.zeros(1, np.int32)
+            k = 0
+        else:
+            k = len(src)
+        t = ctypes.c_uint64()
+        st = lib().pgd_server_submit(self.h, src, dst, k, n_min, ctypes.byref(t))
+        if st:
+            raise PGDError(st, "pgd_server_submit failed")
+        return t.value
+
+    def poll(self, ticket):
+        """None while running, else (status, Counts)."""
+        c = pgd_counts()
+        done = ctypes.c_int()
+        st = lib().pgd_server_poll(self.h, ticket, ctypes.byref(c), ctypes.byref(done))
+        return (st, Counts(c)) if done.value else None
+
+    def wait(self, ticket, timeout_ms=60000):
+        """(status, Counts); status PGD_ETIMEOUT (3) leaves the request running."""
+        c = pgd_counts()
+        st = lib().pgd_server_wait(self.h, ticket, timeout_ms, ctypes.byref(c))
+        return st, Counts(c)
+
+    def stats(self):
+        s = pgd_server_stat()
+        lib().pgd_server_stats(self.h, ctypes.byref(s))
+        return {f: getattr(s, f) for f, _ in pgd_server_stat._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().pgd_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------

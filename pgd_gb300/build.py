@@ -38,7 +38,7 @@ CUDA = cuda_home()
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 
 CU_SOURCES = ["graph_build.cu", "decompose.cu"]
-CPP_SOURCES = ["api.cpp", "reader.cpp", "closing.cpp", "gen.cpp"]
+CPP_SOURCES = ["api.cpp", "reader.cpp", "closing.cpp", "gen.cpp", "serve.cpp"]
 CLI_SOURCES = ["graphlet_core.cpp", "pgd_cli.cpp"]
 
 

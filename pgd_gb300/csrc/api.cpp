@@ -163,6 +163,8 @@ extern "C" pgd_status pgd_graph_destroy(pgd_graph *g) {
     pgd_graph_free(g, g->offp, (g->n + 1) * sizeof(int64_t));
     pgd_graph_free(g, g->adjp, (g->m + 1) * sizeof(int32_t));
     pgd_graph_free(g, g->hubid, (g->n + 1) * sizeof(int32_t));
+    pgd_graph_free(g, g->vrank, (g->n + 1) * sizeof(int32_t));
+    pgd_graph_free(g, g->adjp_rank, (g->m + 1) * sizeof(int32_t));
     pgd_graph_free(g, g->tslot, (2 * g->m + 1) * sizeof(uint32_t));
     // whatever is left (partial builds) is returned to the budget as well
     g->ctx->resident -= g->bytes;
@@ -384,9 +386,84 @@ extern "C" pgd_status pgd_get_micro(pgd_graph *g, int64_t *src1, int64_t *dst1, 
 extern "C" pgd_status pgd_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k, uint32_t flags,
                                           pgd_counts *out) {
     if (!ctx || k < 0 || (k > 0 && (!graphs || !out))) return pgd_fail(ctx, PGD_EINVAL, "bad arguments");
+    if (k == 0) return PGD_OK;
+    cudaSetDevice(ctx->device);
+    pgd_status st;
     for (int i = 0; i < k; i++) {
-        pgd_status st = pgd_decompose(graphs[i], flags, &out[i]);
-        if (st) return st;
+        pgd_graph *g = graphs[i];
+        if (!g || g->ctx != ctx) return pgd_fail(ctx, PGD_EINVAL, "batch graph is null or from another context");
+        if (!g->preprocessed && (st = pgd_preprocess(g, "deg", 0))) return st;
+        if (!g->sorted && (st = pgd_sort_edges(g, "deg", 0))) return st;
     }
+    return pgd_dev_decompose_batch(ctx, graphs, k, (flags & PGD_MICRO) != 0, out);
+}
+
+extern "C" pgd_status pgd_set_thresholds(pgd_ctx *ctx, int anchor_hub, int cache_hub, int dense_max) {
+    if (!ctx) return PGD_EINVAL;
+    if (anchor_hub < 2 || anchor_hub > 256 || cache_hub < 2 || dense_max < 0 || dense_max > 2048)
+        return pgd_fail(ctx, PGD_EINVAL,
+                        "thresholds out of range (2 <= anchor_hub <= 256, cache_hub >= 2, 0 <= dense_max <= 2048)");
+    ctx->anchor_hub = anchor_hub;
+    ctx->cache_hub = cache_hub;
+    ctx->dense_max = dense_max;
+    return PGD_OK;
+}
+
+extern "C" pgd_status pgd_get_thresholds(const pgd_ctx *ctx, int *anchor_hub, int *cache_hub, int *dense_max) {
+    if (!ctx) return PGD_EINVAL;
+    if (anchor_hub) *anchor_hub = ctx->anchor_hub;
+    if (cache_hub) *cache_hub = ctx->cache_hub;
+    if (dense_max) *dense_max = ctx->dense_max;
+    return PGD_OK;
+}
+
+extern "C" pgd_status pgd_autotune(pgd_ctx *ctx, pgd_graph *const *graphs, int k, int reps, int *anchor_hub,
+                                   int *cache_hub, int *dense_max, float *best_ms) {
+    if (!ctx || k <= 0 || !graphs) return pgd_fail(ctx, PGD_EINVAL, "bad arguments");
+    if (reps < 1) reps = 1;
+    std::vector<pgd_counts> out((size_t)k);
+    std::vector<uint64_t> first;
+    // times one candidate; every candidate must give the same counts
+    auto trial = [&](float *ms) -> pgd_status {
+        float total = 0;
+        for (int r = 0; r < reps; r++) {
+            pgd_status st = pgd_decompose_batch(ctx, graphs, k, 0, out.data());
+            if (st) return st;
+            total += out[0].kernel_ms;
+        }
+        std::vector<uint64_t> now;
+        for (int i = 0; i < k; i++) now.insert(now.end(), out[(size_t)i].totals, out[(size_t)i].totals + PGD_NTOTALS);
+        if (first.empty()) first = now;
+        else if (first != now) return pgd_fail(ctx, PGD_EINVAL, "thresholds changed a count (internal error)");
+        *ms = total / reps;
+        return PGD_OK;
+    };
+    // 1. the bitset/list crossover for small graphs, 2. the two hub thresholds
+    float best = -1, ms = 0;
+    int bd = ctx->dense_max;
+    for (int d : {0, 256, 1024, 2048}) {
+        ctx->dense_max = d;
+        pgd_status st = trial(&ms);
+        if (st) return st;
+        if (best < 0 || ms < best) { best = ms; bd = d; }
+    }
+    ctx->dense_max = bd;
+    best = -1;
+    int ba = ctx->anchor_hub, bc = ctx->cache_hub;
+    for (int a : {32, 64, 128, 256}) {
+        for (int c : {32, 64, 128, 512}) {
+            ctx->anchor_hub = a;
+            ctx->cache_hub = c;
+            pgd_status st = trial(&ms);
+            if (st) return st;
+            if (best < 0 || ms < best) { best = ms; ba = a; bc = c; }
+        }
+    }
+    ctx->anchor_hub = ba;
+    ctx->cache_hub = bc;
+    if (anchor_hub) *anchor_hub = ba;
+    if (cache_hub) *cache_hub = bc;
+    if (dense_max) *dense_max = bd;
+    if (best_ms) *best_ms = best;
     return PGD_OK;
 }

@@ -42,6 +42,7 @@
 #include <cub/cub.cuh>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "pgd_internal.h"
 #include "pgd_kernels.cuh"
@@ -51,8 +52,9 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kHubWarps = 16;            // hub-anchor CTA: 512 threads
 constexpr int kLightWarps = 8;           // light path: 256 threads, one edge per warp
-constexpr int kAnchorHub = 128;          // anchors of degree >= this take the bitmap path
-constexpr int kCacheHub = 64;            // W(w,p) cached for neighbours of degree >= this
+constexpr int kAnchorHub = 128;          // default: anchors of degree >= this take the bitmap path
+constexpr int kCacheHub = 64;            // default: W(w,p) cached for neighbours of degree >= this
+constexpr int kLightStageMax = 256;      // largest warp/block threshold the light path can stage
 constexpr int kChunk = 2048;             // max edges of one anchor per CTA work item
 constexpr uint32_t kPending = 0xffffffffu;
 constexpr int kMaxSmemBitmap = 160 * 1024;
@@ -77,8 +79,18 @@ struct DevGraph {
     const int32_t *order;
     long long n, m;
     uint64_t *micro;
-    unsigned long long *sums;
+    unsigned long long *sums;   // PGD_NSUMS, or PGD_NSUMS per graph when batched
+    const int32_t *egraph;      // batched: graph of each E_ordered position, else null
+    const long long *gnm;       // batched: n and m of each graph
+    const uint8_t *gdense;      // batched: graph decomposed by the row-bitset kernel
+    const int32_t *vrank;       // rank of each vertex by (degree desc, id)
+    const int32_t *adjp_rank;   // vrank of each entry of adjp
+    int anchor_hub;             // anchors of degree >= this take the bitmap path
 };
+
+__device__ __forceinline__ bool dense_edge(const DevGraph &G, int64_t e) {
+    return G.gdense && G.gdense[G.egraph[e]];
+}
 
 __device__ __forceinline__ bool ranks_above(int32_t a, int32_t b, const int32_t *deg) {
     int da = deg[a], db = deg[b];
@@ -113,9 +125,25 @@ __global__ void k_oriented_fill(const int64_t *off, const int32_t *adj, const ui
         offp[v] = pos[v < n ? off[v] : nnz];
 }
 
-__global__ void k_hub_flags(const int32_t *deg, int64_t n, uint32_t *flag) {
+// degree rank: position in the order (degree descending, id ascending)
+__global__ void k_rank_keys(const int32_t *deg, int64_t n, uint64_t *keys) {
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
-        flag[v] = deg[v] >= kCacheHub ? 1u : 0u;
+        keys[v] = ((uint64_t)(uint32_t)(0x7fffffff - deg[v]) << 32) | (uint32_t)v;
+}
+
+__global__ void k_rank_scatter(const uint64_t *sorted, int64_t n, int32_t *vrank) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        vrank[(uint32_t)(sorted[i] & 0xffffffffu)] = (int32_t)i;
+}
+
+__global__ void k_gather_rank(const int32_t *adjp, const int32_t *vrank, int64_t m, int32_t *out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = vrank[adjp[i]];
+}
+
+__global__ void k_hub_flags(const int32_t *deg, int64_t n, int cache_hub, uint32_t *flag) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        flag[v] = deg[v] >= cache_hub ? 1u : 0u;
 }
 
 __global__ void k_hub_ids(const uint32_t *flag, const uint32_t *pos, int64_t n, int32_t *hubid) {
@@ -129,6 +157,9 @@ __global__ void k_tslot(DevGraph G, uint32_t *tslot) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t id = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; id < G.m; id += nw) {
+        // in a batch each graph's edge ids and E_ordered positions cover the
+        // same range, so egraph[id] is the edge's graph
+        if (dense_edge(G, id)) continue;
         const int32_t a = G.ev[id], b = G.eu[id];
         const int da = G.deg[a], db = G.deg[b];
         const int32_t s = da <= db ? a : b, l = da <= db ? b : a;
@@ -147,18 +178,27 @@ __global__ void k_tslot(DevGraph G, uint32_t *tslot) {
 
 // key = (anchor << 32 | position) for hub-anchored edges, (~0 << 32 | position)
 // for the rest, so one sort groups the first and lists the second in order.
-__global__ void k_plan_keys(DevGraph G, uint64_t *keys, unsigned long long *nhub) {
-    unsigned long long local = 0;
+// Dense-graph edges (batches only) get 0xfffffffe, so the sorted order is
+// [hub-anchored, by anchor][dense][light].
+__global__ void k_plan_keys(DevGraph G, uint64_t *keys, unsigned long long *counts) {
+    unsigned long long hubs = 0, dense = 0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < G.m; e += (int64_t)gridDim.x * blockDim.x) {
         const int32_t id = G.order[e];
         const int32_t v = G.ev[id], u = G.eu[id];
         const int32_t p = ranks_above(v, u, G.deg) ? v : u;
-        const bool hub = G.deg[p] >= kAnchorHub;
-        keys[e] = ((uint64_t)(hub ? (uint32_t)p : 0xffffffffu) << 32) | (uint32_t)e;
-        local += hub;
+        const bool d = dense_edge(G, e);
+        const bool hub = !d && G.deg[p] >= G.anchor_hub;
+        const uint32_t hi = d ? 0xfffffffeu : (hub ? (uint32_t)p : 0xffffffffu);
+        keys[e] = ((uint64_t)hi << 32) | (uint32_t)e;
+        hubs += hub;
+        dense += d;
     }
-    local = pgd_warp_sum(local);
-    if ((threadIdx.x & 31) == 0 && local) atomicAdd(nhub, local);
+    hubs = pgd_warp_sum(hubs);
+    dense = pgd_warp_sum(dense);
+    if ((threadIdx.x & 31) == 0) {
+        if (hubs) atomicAdd(counts, hubs);
+        if (dense) atomicAdd(counts + 3, dense);
+    }
 }
 
 // item i starts a chunk: first edge of an anchor, or every kChunk-th of it
@@ -189,21 +229,47 @@ __global__ void k_keys_pos(const uint64_t *keys, int64_t n, int32_t *posv) {
 // ---------------------------------------------------------------------------
 // shared per-edge epilogue
 
-__device__ __forceinline__ void edge_epilogue(const DevGraph &G, unsigned long long *acc, int64_t e, int32_t v,
-                                              int32_t u, unsigned long long t, unsigned long long k4,
+__device__ __forceinline__ void flush_graph(const DevGraph &G, unsigned long long *acc, int g) {
+    unsigned long long *dst = G.sums + (int64_t)g * PGD_NSUMS;
+#pragma unroll
+    for (int i = 0; i < PGD_NSUMS; i++) {
+        if (acc[i]) atomicAdd(dst + i, acc[i]);
+        acc[i] = 0;
+    }
+}
+
+// Closed forms, sums and the per-edge row of one edge.  Batched runs keep
+// the sums of the current graph in acc and flush them when the warp moves
+// on to another graph (cur_g).
+__device__ __forceinline__ void edge_epilogue(const DevGraph &G, unsigned long long *acc, int &cur_g, int64_t e,
+                                              int32_t v, int32_t u, unsigned long long t, unsigned long long k4,
                                               unsigned long long c4, int lane) {
     const long long dv = G.deg[v], du = G.deg[u];
+    long long n = G.n, m = G.m;
+    if (G.egraph) {
+        const int g = G.egraph[e];
+        if (g != cur_g) {
+            if (lane == 0 && cur_g >= 0) flush_graph(G, acc, cur_g);
+            cur_g = g;
+        }
+        n = G.gnm[2 * g];
+        m = G.gnm[2 * g + 1];
+    }
     if (lane == 0) {
-        pgd_edge_sums(acc, dv, du, t, G.m, G.n);
+        pgd_edge_sums(acc, dv, du, t, m, n);
         acc[3] += k4;
         acc[4] += c4;
     }
     if (G.micro && lane < PGD_NMICRO) G.micro[e * PGD_NMICRO + lane] = pgd_micro_col(lane, dv, du, t, k4, c4);
 }
 
-__device__ __forceinline__ void block_flush(unsigned long long *acc, unsigned long long (*red)[PGD_NSUMS], int nwarps,
-                                            unsigned long long *sums) {
+__device__ __forceinline__ void block_flush(const DevGraph &G, unsigned long long *acc, int cur_g,
+                                            unsigned long long (*red)[PGD_NSUMS], int nwarps) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (G.egraph) {
+        if (lane == 0 && cur_g >= 0) flush_graph(G, acc, cur_g);
+        return;
+    }
     if (lane == 0) {
 #pragma unroll
         for (int i = 0; i < PGD_NSUMS; i++) red[wid][i] = acc[i];
@@ -212,7 +278,7 @@ __device__ __forceinline__ void block_flush(unsigned long long *acc, unsigned lo
     if (threadIdx.x < PGD_NSUMS) {
         unsigned long long s = 0;
         for (int w = 0; w < nwarps; w++) s += red[w][threadIdx.x];
-        atomicAdd(sums + threadIdx.x, s);
+        atomicAdd(G.sums + threadIdx.x, s);
     }
 }
 
@@ -243,7 +309,7 @@ __device__ __forceinline__ bool bit_of(const uint32_t *bm, int32_t x) { return (
 // entries are read warp-cooperatively with four loads in flight per lane;
 // shorter ones are flattened across the warp.
 
-constexpr int kTCap = 512;               // T entries kept in shared memory per warp
+constexpr int kRankBits = 16384;         // T members of degree rank below this are marked in a per-warp bitmap
 constexpr int kQueue = 2048;             // queued W computations per CTA
 
 struct HubArgs {
@@ -271,24 +337,31 @@ __device__ __forceinline__ unsigned count_bits(const uint32_t *bm, const int32_t
     return c;
 }
 
-// y in T: T sorted in shared memory (small T) or N(q) searched in global memory.
-__device__ __forceinline__ bool in_t(const int32_t *Ts, int t, bool small, const int32_t *Nq, int dq, int32_t y) {
-    return small ? pgd_contains(Ts, t, y) : pgd_contains(Nq, dq, y);
+// y in T = N(p) n N(q).  Almost every y tested is a high-degree vertex, so
+// T's members of degree rank < kRankBits are marked in a per-warp bitmap and
+// the test is one shared-memory bit; other y fall back to the p bitmap and a
+// search of N(q).
+__device__ __forceinline__ bool in_t(const uint32_t *Rw, const uint32_t *bm, const int32_t *Nq, int dq, int32_t y,
+                                     int32_t ry) {
+    if (ry < kRankBits) return (Rw[ry >> 5] >> (ry & 31)) & 1u;
+    return bit_of(bm, y) && pgd_contains(Nq, dq, y);
 }
 
 __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
     extern __shared__ uint32_t s_bits[];
     __shared__ unsigned long long s_red[kHubWarps][PGD_NSUMS];
-    __shared__ int32_t s_T[kHubWarps][kTCap];
+    __shared__ uint32_t s_R[kHubWarps][kRankBits / 32];
     __shared__ int32_t s_qw[kQueue];
     __shared__ int32_t s_qh[kQueue];
     __shared__ long long s_item;
     __shared__ int s_qlen, s_qnext, s_enext_a, s_enext_c;
     const DevGraph &G = A.G;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int32_t *Ts = s_T[wid];
+    uint32_t *Rw = s_R[wid];
+    for (int i = lane; i < kRankBits / 32; i += 32) Rw[i] = 0;
     uint32_t *bm = A.smem_bitmap ? s_bits : A.gbitmap + (int64_t)blockIdx.x * A.nwords;
     unsigned long long *cache = A.cache + (int64_t)blockIdx.x * A.nhubs;
+    int cur_g = -1;
     unsigned long long acc[PGD_NSUMS];
 #pragma unroll
     for (int i = 0; i < PGD_NSUMS; i++) acc[i] = 0;
@@ -406,31 +479,29 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
             for (int base = 0; base < dq; base += 32) {
                 const int j = base + lane;
                 bool inT = false;
-                int32_t w = -1;
                 if (j < dq) {
-                    w = __ldg(Nq + j);
+                    const int32_t w = __ldg(Nq + j);
                     if (w != p) {
                         if (bit_of(bm, w)) {
                             inT = true;
                             sumtq += G.tslot[offq + j];
+                            const int32_t r = G.vrank[w];
+                            if (r < kRankBits) atomicOr(Rw + (r >> 5), 1u << (r & 31));
                         } else {
                             const int32_t h = G.hubid[w];
                             if (h >= 0) sumW += (uint32_t)cache[h];
                         }
                     }
                 }
-                const unsigned mask = __ballot_sync(0xffffffffu, inT);
-                const unsigned at = t + __popc(mask & ((1u << lane) - 1));
-                if (inT && at < (unsigned)kTCap) Ts[at] = w;
-                t += __popc(mask);
+                t += __popc(__ballot_sync(0xffffffffu, inT));
             }
             __syncwarp();
-            const bool tsmall = t <= (unsigned)kTCap;
             // pass 2: scan N(w) of non-hub w in S_q and N+(x) of x in T
             for (int base = 0; base < dq; base += 32) {
                 const int j = base + lane;
                 int len = 0, kind = 0;
                 const int32_t *list = nullptr;
+                const int32_t *rlist = nullptr;
                 if (j < dq) {
                     const int32_t w = __ldg(Nq + j);
                     if (w != p) {
@@ -439,6 +510,7 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                             const int64_t o = G.offp[w];
                             len = (int)(G.offp[w + 1] - o);
                             list = G.adjp + o;
+                            rlist = G.adjp_rank + o;
                         } else if (G.hubid[w] < 0) {
                             len = G.deg[w];
                             list = G.adj + G.off[w];
@@ -451,14 +523,18 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                     const int src = __ffs(longm) - 1;
                     longm &= longm - 1;
                     const int32_t *L = (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)list, src);
+                    const int32_t *LR = (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)rlist, src);
                     const int ln = __shfl_sync(0xffffffffu, len, src);
                     if (__shfl_sync(0xffffffffu, kind, src) == 0) {
                         sumW += count_bits(bm, L, ln, lane);
                     } else {
-                        for (int i = lane; i < ln; i += 32) {
-                            const int32_t y = __ldg(L + i);
-                            k4 += (bit_of(bm, y) && in_t(Ts, (int)t, tsmall, Nq, dq, y)) ? 1 : 0;
+                        int i = lane;
+                        for (; i + 32 < ln; i += 64) {
+                            const int32_t y0 = __ldg(L + i), y1 = __ldg(L + i + 32);
+                            const int32_t r0 = __ldg(LR + i), r1 = __ldg(LR + i + 32);
+                            k4 += (in_t(Rw, bm, Nq, dq, y0, r0) ? 1 : 0) + (in_t(Rw, bm, Nq, dq, y1, r1) ? 1 : 0);
                         }
+                        for (; i < ln; i += 32) k4 += in_t(Rw, bm, Nq, dq, __ldg(L + i), __ldg(LR + i)) ? 1 : 0;
                     }
                 }
                 // short lists: flattened over the warp
@@ -471,12 +547,14 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                     const int own = owner_of(incl, it);
                     const int32_t *olist =
                         (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)list, own);
+                    const int32_t *orank =
+                        (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)rlist, own);
                     const int okind = __shfl_sync(0xffffffffu, kind, own);
                     const int oexcl = __shfl_sync(0xffffffffu, excl, own);
                     if (it < total) {
                         const int32_t x = __ldg(olist + (it - oexcl));
                         if (okind == 0) sumW += bit_of(bm, x);
-                        else k4 += (bit_of(bm, x) && in_t(Ts, (int)t, tsmall, Nq, dq, x)) ? 1 : 0;
+                        else k4 += in_t(Rw, bm, Nq, dq, x, __ldg(orank + (it - oexcl))) ? 1 : 0;
                     }
                 }
             }
@@ -485,14 +563,16 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
             k4 = pgd_warp_sum(k4);
             const long long c4 = (long long)sumW - ((long long)dq - (long long)t - 1) - (long long)sumtq +
                                  2 * (long long)k4 + (long long)t;
-            edge_epilogue(G, acc, e, v, u, t, k4, (unsigned long long)c4, lane);
+            edge_epilogue(G, acc, cur_g, e, v, u, t, k4, (unsigned long long)c4, lane);
+            __syncwarp();
+            for (int i = lane; i < kRankBits / 32; i += 32) Rw[i] = 0;
             __syncwarp();
         }
         __syncthreads();
         for (int i = threadIdx.x; i < dp; i += blockDim.x) bm[__ldg(Np + i) >> 5] = 0;
         __syncthreads();
     }
-    block_flush(acc, s_red, kHubWarps, G.sums);
+    block_flush(G, acc, cur_g, s_red, kHubWarps);
 }
 
 // ---------------------------------------------------------------------------
@@ -507,23 +587,29 @@ struct LightArgs {
 };
 
 __global__ void __launch_bounds__(kLightWarps * 32) k_light(LightArgs A) {
-    __shared__ int32_t s_np[kLightWarps][kAnchorHub];
-    __shared__ uint8_t s_lab[kLightWarps][kAnchorHub];
+    __shared__ int32_t s_np[kLightWarps][kLightStageMax];
+    __shared__ uint8_t s_lab[kLightWarps][kLightStageMax];
     __shared__ unsigned long long s_red[kLightWarps][PGD_NSUMS];
     const DevGraph &G = A.G;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     int32_t *np_s = s_np[wid];
     uint8_t *lab_s = s_lab[wid];
+    int cur_g = -1;
     unsigned long long acc[PGD_NSUMS];
 #pragma unroll
     for (int i = 0; i < PGD_NSUMS; i++) acc[i] = 0;
 
+    // edges are fetched four at a time: neighbouring positions mostly belong
+    // to the same graph when a batch is decomposed
+    unsigned long long idx = 0, idx_end = 0;
     while (true) {
-        unsigned long long idx = 0;
-        if (lane == 0) idx = atomicAdd(A.next, 1ull);
-        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if (idx == idx_end) {
+            if (lane == 0) idx = atomicAdd(A.next, 4ull);
+            idx = __shfl_sync(0xffffffffu, idx, 0);
+            idx_end = min(idx + 4, (unsigned long long)A.nlight);
+        }
         if (idx >= (unsigned long long)A.nlight) break;
-        const int64_t e = A.lpos[idx];
+        const int64_t e = A.lpos[idx++];
         const int32_t id = G.order[e];
         const int32_t v = G.ev[id], u = G.eu[id];
         const int32_t p = ranks_above(v, u, G.deg) ? v : u;
@@ -598,10 +684,114 @@ __global__ void __launch_bounds__(kLightWarps * 32) k_light(LightArgs A) {
         k4 = pgd_warp_sum(k4);
         const long long c4 = (long long)sumW - ((long long)dq - (long long)t - 1) - (long long)sumtq +
                              2 * (long long)k4 + (long long)t;
-        edge_epilogue(G, acc, e, v, u, t, k4, (unsigned long long)c4, lane);
+        edge_epilogue(G, acc, cur_g, e, v, u, t, k4, (unsigned long long)c4, lane);
         __syncwarp();
     }
-    block_flush(acc, s_red, kLightWarps, G.sums);
+    block_flush(G, acc, cur_g, s_red, kLightWarps);
+}
+
+// ---------------------------------------------------------------------------
+// Small graphs (batches): one warp per edge with whole adjacency rows as
+// bitsets.  A row of up to 2048 vertices is 32 words of 64 bits, one per
+// lane, so with A_x the row of x, T = A_p & A_q,
+// S_p = A_p & ~A_q & ~{q}, S_q = A_q & ~A_p & ~{p}:
+//   t = popc(T),  c4 = sum_{w in S_q} popc(A_w & S_p),
+//   k4 = 1/2 sum_{x in T} popc(A_x & T),
+// each row read once, coalesced, from L2.
+
+struct DenseArgs {
+    DevGraph G;
+    const uint64_t *bits;     // rows of every dense graph, concatenated
+    const int64_t *wbase;     // per graph: first word of its rows
+    const int64_t *vbase;     // per graph: first union vertex id
+    const int32_t *dpos;      // E_ordered positions of dense-graph edges
+    int64_t ndense;
+    unsigned long long *next;
+};
+
+__global__ void k_dense_bits(const int64_t *off, const int32_t *adj, const int32_t *vgraph, const uint8_t *gdense,
+                             const int64_t *wbase, const int64_t *vbase, const long long *gnm, int64_t N,
+                             unsigned long long *bits) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t x = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; x < N; x += nw) {
+        const int g = vgraph[x];
+        if (!gdense[g]) continue;
+        const int64_t W = (gnm[2 * g] + 63) >> 6, vb = vbase[g];
+        unsigned long long *row = bits + wbase[g] + (x - vb) * W;
+        for (int64_t j = off[x] + lane; j < off[x + 1]; j += 32) {
+            const int64_t c = adj[j] - vb;
+            atomicOr(row + (c >> 6), 1ull << (c & 63));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_dense(DenseArgs A) {
+    __shared__ unsigned long long s_red[8][PGD_NSUMS];
+    const DevGraph &G = A.G;
+    const int lane = threadIdx.x & 31;
+    int cur_g = -1;
+    unsigned long long acc[PGD_NSUMS];
+#pragma unroll
+    for (int i = 0; i < PGD_NSUMS; i++) acc[i] = 0;
+    unsigned long long idx = 0, idx_end = 0;
+    while (true) {
+        if (idx == idx_end) {
+            if (lane == 0) idx = atomicAdd(A.next, 4ull);
+            idx = __shfl_sync(0xffffffffu, idx, 0);
+            idx_end = min(idx + 4, (unsigned long long)A.ndense);
+        }
+        if (idx >= (unsigned long long)A.ndense) break;
+        const int64_t e = A.dpos[idx++];
+        const int32_t id = G.order[e];
+        const int32_t v = G.ev[id], u = G.eu[id];
+        const int g = G.egraph[e];
+        const int64_t vb = A.vbase[g];
+        const int W = (int)((G.gnm[2 * g] + 63) >> 6);
+        const uint64_t *rows = A.bits + A.wbase[g];
+        // scan the endpoint of smaller degree: |S_q| + t = d_q - 1 rows
+        const bool vq = G.deg[v] <= G.deg[u];
+        const int64_t q = (vq ? v : u) - vb, p = (vq ? u : v) - vb;
+        const uint64_t Ap = lane < W ? __ldg(rows + p * W + lane) : 0ull;
+        const uint64_t Aq = lane < W ? __ldg(rows + q * W + lane) : 0ull;
+        const uint64_t bq = (lane == (int)(q >> 6)) ? (1ull << (q & 63)) : 0ull;
+        const uint64_t bp = (lane == (int)(p >> 6)) ? (1ull << (p & 63)) : 0ull;
+        const uint64_t T = Ap & Aq;
+        const uint64_t Sp = Ap & ~Aq & ~bq;
+        const uint64_t Sq = Aq & ~Ap & ~bp;
+        unsigned long long t = __popcll(T), c4 = 0, k4x2 = 0;
+        for (int L = 0; L < W; L++) {
+            uint64_t ws = __shfl_sync(0xffffffffu, Sq, L);
+            uint64_t wt = __shfl_sync(0xffffffffu, T, L);
+            while (ws) {
+                const int b0 = __ffsll(ws) - 1;
+                ws &= ws - 1;
+                const int64_t w0 = (int64_t)L * 64 + b0;
+                if (ws) {
+                    const int b1 = __ffsll(ws) - 1;
+                    ws &= ws - 1;
+                    const int64_t w1 = (int64_t)L * 64 + b1;
+                    const uint64_t r0 = lane < W ? __ldg(rows + w0 * W + lane) : 0ull;
+                    const uint64_t r1 = lane < W ? __ldg(rows + w1 * W + lane) : 0ull;
+                    c4 += __popcll(r0 & Sp) + __popcll(r1 & Sp);
+                } else {
+                    const uint64_t r0 = lane < W ? __ldg(rows + w0 * W + lane) : 0ull;
+                    c4 += __popcll(r0 & Sp);
+                }
+            }
+            while (wt) {
+                const int b0 = __ffsll(wt) - 1;
+                wt &= wt - 1;
+                const uint64_t r0 = lane < W ? __ldg(rows + ((int64_t)L * 64 + b0) * W + lane) : 0ull;
+                k4x2 += __popcll(r0 & T);
+            }
+        }
+        t = pgd_warp_sum(t);
+        c4 = pgd_warp_sum(c4);
+        k4x2 = pgd_warp_sum(k4x2);
+        edge_epilogue(G, acc, cur_g, e, v, u, t, k4x2 >> 1, c4, lane);
+    }
+    block_flush(G, acc, cur_g, s_red, 8);
 }
 
 }  // namespace
@@ -613,10 +803,14 @@ static pgd_status build_aux(pgd_graph *g) {
     cudaStream_t s = ctx->stream;
     pgd_status st;
     const int64_t n = g->n, nnz = 2 * g->m;
-    if ((st = pgd_graph_alloc(g, (void **)&g->offp, (n + 1) * sizeof(int64_t)))) return st;
-    if ((st = pgd_graph_alloc(g, (void **)&g->adjp, (g->m + 1) * sizeof(int32_t)))) return st;
-    if ((st = pgd_graph_alloc(g, (void **)&g->hubid, (n + 1) * sizeof(int32_t)))) return st;
-    if ((st = pgd_graph_alloc(g, (void **)&g->tslot, (nnz + 1) * sizeof(uint32_t)))) return st;
+    if (!g->offp) {
+        if ((st = pgd_graph_alloc(g, (void **)&g->offp, (n + 1) * sizeof(int64_t)))) return st;
+        if ((st = pgd_graph_alloc(g, (void **)&g->adjp, (g->m + 1) * sizeof(int32_t)))) return st;
+        if ((st = pgd_graph_alloc(g, (void **)&g->vrank, (n + 1) * sizeof(int32_t)))) return st;
+        if ((st = pgd_graph_alloc(g, (void **)&g->adjp_rank, (g->m + 1) * sizeof(int32_t)))) return st;
+        if ((st = pgd_graph_alloc(g, (void **)&g->hubid, (n + 1) * sizeof(int32_t)))) return st;
+        if ((st = pgd_graph_alloc(g, (void **)&g->tslot, (nnz + 1) * sizeof(uint32_t)))) return st;
+    }
     int32_t *row = nullptr;
     uint32_t *flag = nullptr, *pos = nullptr;
     const int64_t len = std::max(nnz, n) + 1;
@@ -636,7 +830,7 @@ static pgd_status build_aux(pgd_graph *g) {
     PGD_LAUNCH(ctx, k_oriented_fill, grid_for(std::max(nnz, n + 1)), kThreads, 0, g->off, g->adj, flag, pos, n, nnz,
                g->offp, g->adjp);
     // hub ids
-    PGD_LAUNCH(ctx, k_hub_flags, grid_for(n), kThreads, 0, g->deg, n, flag);
+    PGD_LAUNCH(ctx, k_hub_flags, grid_for(n), kThreads, 0, g->deg, n, ctx->cache_hub, flag);
     PGD_CUDA(ctx, cudaMemsetAsync(flag + n, 0, sizeof(uint32_t), s));
     tb = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, tb, flag, pos, n + 1, s);
@@ -644,6 +838,24 @@ static pgd_status build_aux(pgd_graph *g) {
     cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, n + 1, s);
     pgd_tmp_free(ctx, tmp);
     PGD_LAUNCH(ctx, k_hub_ids, grid_for(n), kThreads, 0, flag, pos, n, g->hubid);
+    // degree ranks of the vertices and of the oriented list entries
+    {
+        uint64_t *rk = nullptr, *rk2 = nullptr;
+        if ((st = pgd_tmp_alloc(ctx, (void **)&rk, (n + 1) * sizeof(uint64_t)))) return st;
+        if ((st = pgd_tmp_alloc(ctx, (void **)&rk2, (n + 1) * sizeof(uint64_t)))) return st;
+        if (n > 0) {
+            PGD_LAUNCH(ctx, k_rank_keys, grid_for(n), kThreads, 0, g->deg, n, rk);
+            tb = 0;
+            cub::DeviceRadixSort::SortKeys(nullptr, tb, rk, rk2, n, 0, 64, s);
+            if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
+            cub::DeviceRadixSort::SortKeys(tmp, tb, rk, rk2, n, 0, 64, s);
+            pgd_tmp_free(ctx, tmp);
+            PGD_LAUNCH(ctx, k_rank_scatter, grid_for(n), kThreads, 0, rk2, n, g->vrank);
+        }
+        if (g->m > 0) PGD_LAUNCH(ctx, k_gather_rank, grid_for(g->m), kThreads, 0, g->adjp, g->vrank, g->m, g->adjp_rank);
+        pgd_tmp_free(ctx, rk);
+        pgd_tmp_free(ctx, rk2);
+    }
     uint32_t nh = 0;
     PGD_CUDA(ctx, cudaMemcpyAsync(&nh, pos + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     PGD_CUDA(ctx, cudaStreamSynchronize(s));
@@ -652,6 +864,7 @@ static pgd_status build_aux(pgd_graph *g) {
     pgd_tmp_free(ctx, flag);
     pgd_tmp_free(ctx, pos);
     PGD_CUDA(ctx, cudaGetLastError());
+    g->aux_cache_hub = ctx->cache_hub;
     g->has_aux = true;
     return PGD_OK;
 }
@@ -672,7 +885,133 @@ static DevGraph dev_view(pgd_graph *g, bool micro) {
     G.m = g->m;
     G.micro = micro ? g->micro : nullptr;
     G.sums = g->ctx->d_sums;
+    G.egraph = nullptr;
+    G.gnm = nullptr;
+    G.gdense = nullptr;
+    G.vrank = g->vrank;
+    G.adjp_rank = g->adjp_rank;
+    G.anchor_hub = g->ctx->anchor_hub;
     return G;
+}
+
+// Triangle pass, work plan and both decomposition kernels for the graph view
+// G (one graph, or the union of a batch); *ms gets their device time.
+struct DenseView {
+    const uint64_t *bits;
+    const int64_t *wbase;
+    const int64_t *vbase;
+};
+
+static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, uint32_t *tslot, int32_t nhubs, float *ms,
+                                const DenseView *dense = nullptr) {
+    cudaStream_t s = ctx->stream;
+    pgd_status st;
+    const int64_t m = G.m;
+    *ms = 0;
+    if (m == 0) return PGD_OK;
+    uint64_t *keys = nullptr, *keys2 = nullptr;
+    int32_t *posv = nullptr;
+    uint32_t *flag = nullptr, *fpos = nullptr;
+    int64_t *items = nullptr;
+    unsigned long long *cache = nullptr;
+    uint32_t *gbm = nullptr;
+    if ((st = pgd_tmp_alloc(ctx, (void **)&keys, m * sizeof(uint64_t)))) return st;
+    if ((st = pgd_tmp_alloc(ctx, (void **)&keys2, m * sizeof(uint64_t)))) return st;
+    if ((st = pgd_tmp_alloc(ctx, (void **)&posv, m * sizeof(int32_t)))) return st;
+    // [0] hub edges, [1] hub item counter, [2] light counter, [3] dense edges, [4] dense counter
+    unsigned long long *ctr = ctx->d_ctr;
+    PGD_CUDA(ctx, cudaMemsetAsync(ctr, 0, 8 * sizeof(unsigned long long), s));
+    PGD_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
+    PGD_LAUNCH(ctx, k_tslot, grid_for(32 * m), kThreads, 0, G, tslot);
+    PGD_LAUNCH(ctx, k_plan_keys, grid_for(m), kThreads, 0, G, keys, ctr);
+    size_t tb = 0;
+    void *tmp = nullptr;
+    cub::DeviceRadixSort::SortKeys(nullptr, tb, keys, keys2, m, 0, 64, s);
+    if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
+    cub::DeviceRadixSort::SortKeys(tmp, tb, keys, keys2, m, 0, 64, s);
+    pgd_tmp_free(ctx, tmp);
+    PGD_LAUNCH(ctx, k_keys_pos, grid_for(m), kThreads, 0, keys2, m, posv);
+    unsigned long long cnt[4] = {0, 0, 0, 0};
+    PGD_CUDA(ctx, cudaMemcpyAsync(cnt, ctr, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+    PGD_CUDA(ctx, cudaStreamSynchronize(s));
+    const unsigned long long nh = cnt[0], nd = cnt[3];
+    const int64_t nlight = m - (int64_t)nh - (int64_t)nd;
+    int64_t nitems = 0;
+    if (nh > 0) {
+        if ((st = pgd_tmp_alloc(ctx, (void **)&flag, (nh + 1) * sizeof(uint32_t)))) return st;
+        if ((st = pgd_tmp_alloc(ctx, (void **)&fpos, (nh + 1) * sizeof(uint32_t)))) return st;
+        PGD_LAUNCH(ctx, k_item_flags, grid_for(nh), kThreads, 0, keys2, (int64_t)nh, flag);
+        PGD_CUDA(ctx, cudaMemsetAsync(flag + nh, 0, sizeof(uint32_t), s));
+        tb = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, tb, flag, fpos, (int64_t)nh + 1, s);
+        if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
+        cub::DeviceScan::ExclusiveSum(tmp, tb, flag, fpos, (int64_t)nh + 1, s);
+        pgd_tmp_free(ctx, tmp);
+        uint32_t ni = 0;
+        PGD_CUDA(ctx, cudaMemcpyAsync(&ni, fpos + nh, sizeof(ni), cudaMemcpyDeviceToHost, s));
+        PGD_CUDA(ctx, cudaStreamSynchronize(s));
+        nitems = ni;
+        if ((st = pgd_tmp_alloc(ctx, (void **)&items, (nitems + 1) * sizeof(int64_t)))) return st;
+        PGD_LAUNCH(ctx, k_item_fill, grid_for(nh), kThreads, 0, flag, fpos, (int64_t)nh, items);
+    }
+    const int nsm = ctx->num_sms;
+    if (nitems > 0) {
+        const int64_t nwords = (G.n + 31) / 32;
+        const bool in_smem = nwords * 4 <= kMaxSmemBitmap;
+        size_t smem = in_smem ? (size_t)nwords * 4 : 0;
+        const int nh_slots = std::max(1, (int)nhubs);
+        if ((st = pgd_tmp_alloc(ctx, (void **)&cache, (size_t)nsm * nh_slots * sizeof(unsigned long long)))) return st;
+        PGD_CUDA(ctx, cudaMemsetAsync(cache, 0xff, (size_t)nsm * nh_slots * sizeof(unsigned long long), s));
+        if (!in_smem) {
+            if ((st = pgd_tmp_alloc(ctx, (void **)&gbm, (size_t)nsm * nwords * 4))) return st;
+            PGD_CUDA(ctx, cudaMemsetAsync(gbm, 0, (size_t)nsm * nwords * 4, s));
+        }
+        PGD_CUDA(ctx, cudaFuncSetAttribute(k_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        HubArgs H;
+        H.G = G;
+        H.hpos = posv;
+        H.items = items;
+        H.nitems = nitems;
+        H.cache = cache;
+        H.nhubs = nh_slots;
+        H.gbitmap = gbm;
+        H.nwords = nwords;
+        H.smem_bitmap = in_smem ? 1 : 0;
+        H.next = ctr + 1;
+        PGD_LAUNCH(ctx, k_hub, nsm, kHubWarps * 32, smem, H);
+    }
+    if (nd > 0 && dense) {
+        DenseArgs D;
+        D.G = G;
+        D.bits = dense->bits;
+        D.wbase = dense->wbase;
+        D.vbase = dense->vbase;
+        D.dpos = posv + nh;
+        D.ndense = (int64_t)nd;
+        D.next = ctr + 4;
+        PGD_LAUNCH(ctx, k_dense, nsm * 8, 256, 0, D);
+    }
+    if (nlight > 0) {
+        LightArgs L;
+        L.G = G;
+        L.lpos = posv + nh + nd;
+        L.nlight = nlight;
+        L.next = ctr + 2;
+        PGD_LAUNCH(ctx, k_light, nsm * 8, kLightWarps * 32, 0, L);
+    }
+    PGD_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
+    PGD_CUDA(ctx, cudaGetLastError());
+    pgd_tmp_free(ctx, keys);
+    pgd_tmp_free(ctx, keys2);
+    pgd_tmp_free(ctx, posv);
+    pgd_tmp_free(ctx, flag);
+    pgd_tmp_free(ctx, fpos);
+    pgd_tmp_free(ctx, items);
+    pgd_tmp_free(ctx, cache);
+    pgd_tmp_free(ctx, gbm);
+    PGD_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+    PGD_CUDA(ctx, cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
+    return PGD_OK;
 }
 
 pgd_status pgd_dev_decompose(pgd_graph *g, bool micro, pgd_counts *out) {
@@ -682,111 +1021,240 @@ pgd_status pgd_dev_decompose(pgd_graph *g, bool micro, pgd_counts *out) {
     if (micro && !g->micro) {
         if ((st = pgd_graph_alloc(g, (void **)&g->micro, (g->m + 1) * PGD_NMICRO * sizeof(uint64_t)))) return st;
     }
-    if (!g->has_aux && (st = build_aux(g))) return st;
-    const int64_t m = g->m;
+    if ((!g->has_aux || g->aux_cache_hub != ctx->cache_hub) && (st = build_aux(g))) return st;
     PGD_CUDA(ctx, cudaMemsetAsync(ctx->d_sums, 0, PGD_NSUMS * sizeof(unsigned long long), s));
-    DevGraph G = dev_view(g, micro);
     float ms = 0;
-    if (m > 0) {
-        // work plan
-        uint64_t *keys = nullptr, *keys2 = nullptr;
-        int32_t *posv = nullptr;
-        uint32_t *flag = nullptr, *fpos = nullptr;
-        int64_t *items = nullptr;
-        unsigned long long *cache = nullptr;
-        uint32_t *gbm = nullptr;
-        if ((st = pgd_tmp_alloc(ctx, (void **)&keys, m * sizeof(uint64_t)))) return st;
-        if ((st = pgd_tmp_alloc(ctx, (void **)&keys2, m * sizeof(uint64_t)))) return st;
-        if ((st = pgd_tmp_alloc(ctx, (void **)&posv, m * sizeof(int32_t)))) return st;
-        unsigned long long *ctr = ctx->d_ctr;  // [0] hub edges, [1] hub item counter, [2] light counter
-        PGD_CUDA(ctx, cudaMemsetAsync(ctr, 0, 4 * sizeof(unsigned long long), s));
-        PGD_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
-        PGD_LAUNCH(ctx, k_tslot, grid_for(32 * m), kThreads, 0, G, g->tslot);
-        PGD_LAUNCH(ctx, k_plan_keys, grid_for(m), kThreads, 0, G, keys, ctr);
-        size_t tb = 0;
-        void *tmp = nullptr;
-        cub::DeviceRadixSort::SortKeys(nullptr, tb, keys, keys2, m, 0, 64, s);
-        if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
-        cub::DeviceRadixSort::SortKeys(tmp, tb, keys, keys2, m, 0, 64, s);
-        pgd_tmp_free(ctx, tmp);
-        PGD_LAUNCH(ctx, k_keys_pos, grid_for(m), kThreads, 0, keys2, m, posv);
-        unsigned long long nh = 0;
-        PGD_CUDA(ctx, cudaMemcpyAsync(&nh, ctr, sizeof(nh), cudaMemcpyDeviceToHost, s));
-        PGD_CUDA(ctx, cudaStreamSynchronize(s));
-        const int64_t nlight = m - (int64_t)nh;
-        int64_t nitems = 0;
-        if (nh > 0) {
-            if ((st = pgd_tmp_alloc(ctx, (void **)&flag, (nh + 1) * sizeof(uint32_t)))) return st;
-            if ((st = pgd_tmp_alloc(ctx, (void **)&fpos, (nh + 1) * sizeof(uint32_t)))) return st;
-            PGD_LAUNCH(ctx, k_item_flags, grid_for(nh), kThreads, 0, keys2, (int64_t)nh, flag);
-            PGD_CUDA(ctx, cudaMemsetAsync(flag + nh, 0, sizeof(uint32_t), s));
-            tb = 0;
-            cub::DeviceScan::ExclusiveSum(nullptr, tb, flag, fpos, (int64_t)nh + 1, s);
-            if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
-            cub::DeviceScan::ExclusiveSum(tmp, tb, flag, fpos, (int64_t)nh + 1, s);
-            pgd_tmp_free(ctx, tmp);
-            uint32_t ni = 0;
-            PGD_CUDA(ctx, cudaMemcpyAsync(&ni, fpos + nh, sizeof(ni), cudaMemcpyDeviceToHost, s));
-            PGD_CUDA(ctx, cudaStreamSynchronize(s));
-            nitems = ni;
-            if ((st = pgd_tmp_alloc(ctx, (void **)&items, (nitems + 1) * sizeof(int64_t)))) return st;
-            PGD_LAUNCH(ctx, k_item_fill, grid_for(nh), kThreads, 0, flag, fpos, (int64_t)nh, items);
-        }
-        const int nsm = ctx->num_sms;
-        if (nitems > 0) {
-            const int64_t nwords = (g->n + 31) / 32;
-            const bool in_smem = nwords * 4 <= kMaxSmemBitmap;
-            size_t smem = in_smem ? (size_t)nwords * 4 : 0;
-            const int nhubs = std::max(1, (int)g->nhubs);
-            if ((st = pgd_tmp_alloc(ctx, (void **)&cache, (size_t)nsm * nhubs * sizeof(unsigned long long)))) return st;
-            PGD_CUDA(ctx, cudaMemsetAsync(cache, 0xff, (size_t)nsm * nhubs * sizeof(unsigned long long), s));
-            if (!in_smem) {
-                if ((st = pgd_tmp_alloc(ctx, (void **)&gbm, (size_t)nsm * nwords * 4))) return st;
-                PGD_CUDA(ctx, cudaMemsetAsync(gbm, 0, (size_t)nsm * nwords * 4, s));
-            }
-            PGD_CUDA(ctx, cudaFuncSetAttribute(k_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            HubArgs H;
-            H.G = G;
-            H.hpos = posv;
-            H.items = items;
-            H.nitems = nitems;
-            H.cache = cache;
-            H.nhubs = nhubs;
-            H.gbitmap = gbm;
-            H.nwords = nwords;
-            H.smem_bitmap = in_smem ? 1 : 0;
-            H.next = ctr + 1;
-            PGD_LAUNCH(ctx, k_hub, nsm, kHubWarps * 32, smem, H);
-        }
-        if (nlight > 0) {
-            LightArgs L;
-            L.G = G;
-            L.lpos = posv + nh;
-            L.nlight = nlight;
-            L.next = ctr + 2;
-            PGD_LAUNCH(ctx, k_light, nsm * 8, kLightWarps * 32, 0, L);
-        }
-        PGD_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
-        PGD_CUDA(ctx, cudaGetLastError());
-        pgd_tmp_free(ctx, keys);
-        pgd_tmp_free(ctx, keys2);
-        pgd_tmp_free(ctx, posv);
-        pgd_tmp_free(ctx, flag);
-        pgd_tmp_free(ctx, fpos);
-        pgd_tmp_free(ctx, items);
-        pgd_tmp_free(ctx, cache);
-        pgd_tmp_free(ctx, gbm);
-    }
+    if ((st = run_decompose(ctx, dev_view(g, micro), g->tslot, g->nhubs, &ms))) return st;
     unsigned long long h[PGD_NSUMS];
     PGD_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_sums, sizeof(h), cudaMemcpyDeviceToHost, s));
     PGD_CUDA(ctx, cudaStreamSynchronize(s));
-    if (m > 0) PGD_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     for (int i = 0; i < PGD_NSUMS; i++) out->sums[i] = h[i];
     out->n = g->n;
     out->m = g->m;
     out->kernel_ms = ms;
     pgd_close_counts(out->sums, g->n, g->m, out->totals);
     g->has_micro = micro;
+    return PGD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched decomposition: the graphs become one disjoint union on the device
+// (vertex, slot and edge ids offset per graph), decomposed by the same
+// persistent kernels; t, k4 and c4 never cross graphs, the closed forms use
+// each edge's own graph's n and m, and the sums are kept per graph.
+
+struct BatchDesc {
+    const int64_t *off;
+    const int32_t *adj;
+    const int32_t *deg;
+    const int32_t *ev;
+    const int32_t *eu;
+    const int32_t *order;
+    int64_t n, m, vbase, ebase, sbase;   // vertex, edge and slot offsets in the union
+};
+
+__device__ __forceinline__ int batch_find(const int64_t *base, int k, int64_t x) {
+    int lo = 0, hi = k;  // last g with base[g] <= x
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (base[mid] <= x) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_union_vertices(const BatchDesc *D, const int64_t *vbase, int k, int64_t N, int64_t *off,
+                                 int32_t *deg, int32_t *vgraph) {
+    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < N; x += (int64_t)gridDim.x * blockDim.x) {
+        const int g = batch_find(vbase, k, x);
+        const int64_t v = x - D[g].vbase;
+        off[x] = D[g].sbase + D[g].off[v];
+        deg[x] = D[g].deg[v];
+        vgraph[x] = g;
+    }
+}
+
+__global__ void k_union_slots(const BatchDesc *D, const int64_t *sbase, int k, int64_t S, int32_t *adj) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < S; j += (int64_t)gridDim.x * blockDim.x) {
+        const int g = batch_find(sbase, k, j);
+        adj[j] = (int32_t)(D[g].adj[j - D[g].sbase] + D[g].vbase);
+    }
+}
+
+__global__ void k_union_edges(const BatchDesc *D, const int64_t *ebase, int k, int64_t M, int32_t *ev, int32_t *eu,
+                              int32_t *order, int32_t *egraph) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < M; e += (int64_t)gridDim.x * blockDim.x) {
+        const int g = batch_find(ebase, k, e);
+        const int64_t l = e - D[g].ebase;
+        ev[e] = (int32_t)(D[g].ev[l] + D[g].vbase);
+        eu[e] = (int32_t)(D[g].eu[l] + D[g].vbase);
+        order[e] = (int32_t)(D[g].order[l] + D[g].ebase);
+        egraph[e] = g;
+    }
+}
+
+pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k, bool micro, pgd_counts *out) {
+    cudaStream_t s = ctx->stream;
+    pgd_status st;
+    std::vector<BatchDesc> desc((size_t)k);
+    std::vector<int64_t> bases((size_t)3 * k + 3, 0);
+    std::vector<long long> gnm((size_t)2 * k);
+    int64_t N = 0, M = 0, S = 0;
+    for (int i = 0; i < k; i++) {
+        pgd_graph *g = graphs[i];
+        if (micro && !g->micro) {
+            if ((st = pgd_graph_alloc(g, (void **)&g->micro, (g->m + 1) * PGD_NMICRO * sizeof(uint64_t)))) return st;
+        }
+        BatchDesc &d = desc[(size_t)i];
+        d.off = g->off;
+        d.adj = g->adj;
+        d.deg = g->deg;
+        d.ev = g->ev;
+        d.eu = g->eu;
+        d.order = g->order;
+        d.n = g->n;
+        d.m = g->m;
+        d.vbase = N;
+        d.ebase = M;
+        d.sbase = S;
+        bases[(size_t)i] = N;
+        bases[(size_t)k + 1 + i] = M;
+        bases[(size_t)2 * k + 2 + i] = S;
+        gnm[(size_t)2 * i] = g->n;
+        gnm[(size_t)2 * i + 1] = g->m;
+        N += g->n;
+        M += g->m;
+        S += 2 * g->m;
+    }
+    if (N > 0x7ffffffe || S > 0x7fffffff)
+        return pgd_fail(ctx, PGD_EINVAL, "batch too large for 32-bit vertex and slot ids");
+    // the union, as a transient graph of this context
+    pgd_graph U;
+    U.ctx = ctx;
+    U.n = N;
+    U.m = M;
+    BatchDesc *d_desc = nullptr;
+    int64_t *d_bases = nullptr;
+    long long *d_gnm = nullptr;
+    int32_t *egraph = nullptr, *vgraph = nullptr;
+    unsigned long long *gsums = nullptr, *bits = nullptr;
+    uint64_t *umicro = nullptr;
+    uint8_t *d_gdense = nullptr;
+    int64_t *d_wbase = nullptr;
+    // graphs of at most dense_max vertices use the row-bitset kernel
+    std::vector<uint8_t> gdense((size_t)k, 0);
+    std::vector<int64_t> wbase((size_t)k, 0);
+    int64_t words = 0;
+    int ndense_graphs = 0;
+    for (int i = 0; i < k; i++) {
+        const int64_t n = graphs[i]->n;
+        if (n > 0 && n <= ctx->dense_max && graphs[i]->m > 0) {
+            gdense[(size_t)i] = 1;
+            wbase[(size_t)i] = words;
+            words += n * ((n + 63) / 64);
+            ndense_graphs++;
+        }
+    }
+    auto cleanup = [&]() {
+        pgd_tmp_free(ctx, vgraph);
+        pgd_tmp_free(ctx, bits);
+        pgd_tmp_free(ctx, d_gdense);
+        pgd_tmp_free(ctx, d_wbase);
+        pgd_tmp_free(ctx, d_desc);
+        pgd_tmp_free(ctx, d_bases);
+        pgd_tmp_free(ctx, d_gnm);
+        pgd_tmp_free(ctx, egraph);
+        pgd_tmp_free(ctx, gsums);
+        pgd_tmp_free(ctx, umicro);
+        pgd_graph_free(&U, U.off, (N + 1) * sizeof(int64_t));
+        pgd_graph_free(&U, U.adj, (S + 1) * sizeof(int32_t));
+        pgd_graph_free(&U, U.deg, (N + 1) * sizeof(int32_t));
+        pgd_graph_free(&U, U.ev, (M + 1) * sizeof(int32_t));
+        pgd_graph_free(&U, U.eu, (M + 1) * sizeof(int32_t));
+        pgd_graph_free(&U, U.order, (M + 1) * sizeof(int32_t));
+        pgd_graph_free(&U, U.offp, (N + 1) * sizeof(int64_t));
+        pgd_graph_free(&U, U.adjp, (M + 1) * sizeof(int32_t));
+        pgd_graph_free(&U, U.hubid, (N + 1) * sizeof(int32_t));
+        pgd_graph_free(&U, U.vrank, (N + 1) * sizeof(int32_t));
+        pgd_graph_free(&U, U.adjp_rank, (M + 1) * sizeof(int32_t));
+        pgd_graph_free(&U, U.tslot, (S + 1) * sizeof(uint32_t));
+    };
+#define BATCH_TRY(expr)                      \
+    do {                                     \
+        if ((st = (expr)) != PGD_OK) {       \
+            cleanup();                       \
+            return st;                       \
+        }                                    \
+    } while (0)
+    BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&d_desc, (size_t)k * sizeof(BatchDesc)));
+    BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&d_bases, bases.size() * sizeof(int64_t)));
+    BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&d_gnm, gnm.size() * sizeof(long long)));
+    BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&egraph, (M + 1) * sizeof(int32_t)));
+    BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&vgraph, (N + 1) * sizeof(int32_t)));
+    BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&d_gdense, (size_t)k));
+    BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&d_wbase, (size_t)k * sizeof(int64_t)));
+    if (words > 0) BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&bits, (size_t)words * sizeof(unsigned long long)));
+    BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&gsums, (size_t)k * PGD_NSUMS * sizeof(unsigned long long)));
+    if (micro) BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&umicro, (M + 1) * PGD_NMICRO * sizeof(uint64_t)));
+    BATCH_TRY(pgd_graph_alloc(&U, (void **)&U.off, (N + 1) * sizeof(int64_t)));
+    BATCH_TRY(pgd_graph_alloc(&U, (void **)&U.adj, (S + 1) * sizeof(int32_t)));
+    BATCH_TRY(pgd_graph_alloc(&U, (void **)&U.deg, (N + 1) * sizeof(int32_t)));
+    BATCH_TRY(pgd_graph_alloc(&U, (void **)&U.ev, (M + 1) * sizeof(int32_t)));
+    BATCH_TRY(pgd_graph_alloc(&U, (void **)&U.eu, (M + 1) * sizeof(int32_t)));
+    BATCH_TRY(pgd_graph_alloc(&U, (void **)&U.order, (M + 1) * sizeof(int32_t)));
+    if (cudaMemcpyAsync(d_desc, desc.data(), (size_t)k * sizeof(BatchDesc), cudaMemcpyHostToDevice, s) ||
+        cudaMemcpyAsync(d_bases, bases.data(), bases.size() * sizeof(int64_t), cudaMemcpyHostToDevice, s) ||
+        cudaMemcpyAsync(d_gnm, gnm.data(), gnm.size() * sizeof(long long), cudaMemcpyHostToDevice, s) ||
+        cudaMemsetAsync(gsums, 0, (size_t)k * PGD_NSUMS * sizeof(unsigned long long), s) ||
+        cudaMemcpyAsync(d_gdense, gdense.data(), (size_t)k, cudaMemcpyHostToDevice, s) ||
+        cudaMemcpyAsync(d_wbase, wbase.data(), (size_t)k * sizeof(int64_t), cudaMemcpyHostToDevice, s) ||
+        (words > 0 && cudaMemsetAsync(bits, 0, (size_t)words * sizeof(unsigned long long), s))) {
+        cleanup();
+        return pgd_fail(ctx, PGD_ECUDA, "batch set-up copy failed");
+    }
+    PGD_LAUNCH(ctx, k_union_vertices, grid_for(N), kThreads, 0, d_desc, d_bases, k, N, U.off, U.deg, vgraph);
+    PGD_CUDA(ctx, cudaMemcpyAsync(U.off + N, &S, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    PGD_LAUNCH(ctx, k_union_slots, grid_for(S), kThreads, 0, d_desc, d_bases + 2 * k + 2, k, S, U.adj);
+    PGD_LAUNCH(ctx, k_union_edges, grid_for(M), kThreads, 0, d_desc, d_bases + k + 1, k, M, U.ev, U.eu, U.order,
+               egraph);
+    BATCH_TRY(build_aux(&U));
+    if (words > 0)
+        PGD_LAUNCH(ctx, k_dense_bits, grid_for(32 * N), kThreads, 0, U.off, U.adj, vgraph, d_gdense, d_wbase, d_bases,
+                   d_gnm, N, bits);
+    DevGraph G = dev_view(&U, micro);
+    G.micro = micro ? umicro : nullptr;
+    G.sums = gsums;
+    G.egraph = egraph;
+    G.gnm = d_gnm;
+    G.gdense = ndense_graphs ? d_gdense : nullptr;
+    DenseView dv{(const uint64_t *)bits, d_wbase, d_bases};
+    float ms = 0;
+    BATCH_TRY(run_decompose(ctx, G, U.tslot, U.nhubs, &ms, ndense_graphs ? &dv : nullptr));
+    std::vector<unsigned long long> h((size_t)k * PGD_NSUMS);
+    if (cudaMemcpyAsync(h.data(), gsums, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s)) {
+        cleanup();
+        return pgd_fail(ctx, PGD_ECUDA, "batch result copy failed");
+    }
+    for (int i = 0; micro && i < k; i++) {
+        pgd_graph *g = graphs[i];
+        if (g->m && cudaMemcpyAsync(g->micro, umicro + desc[(size_t)i].ebase * PGD_NMICRO,
+                                    g->m * PGD_NMICRO * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s)) {
+            cleanup();
+            return pgd_fail(ctx, PGD_ECUDA, "batch micro copy failed");
+        }
+    }
+    PGD_CUDA(ctx, cudaStreamSynchronize(s));
+    for (int i = 0; i < k; i++) {
+        pgd_counts &o = out[i];
+        memset(&o, 0, sizeof(o));
+        for (int j = 0; j < PGD_NSUMS; j++) o.sums[j] = h[(size_t)i * PGD_NSUMS + j];
+        o.n = gnm[(size_t)2 * i];
+        o.m = gnm[(size_t)2 * i + 1];
+        o.kernel_ms = ms;
+        pgd_close_counts(o.sums, o.n, o.m, o.totals);
+        graphs[i]->has_micro = micro;
+    }
+    cleanup();
+#undef BATCH_TRY
     return PGD_OK;
 }
 
@@ -922,8 +1390,8 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     // CUB temporary storage sizes (queries only)
     size_t tb_scan = 0, tb_sort = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, tb_scan, (uint32_t *)nullptr, (uint32_t *)nullptr, std::max(nnz, n) + 1, s);
-    cub::DeviceRadixSort::SortKeys(nullptr, tb_sort, (uint64_t *)nullptr, (uint64_t *)nullptr, std::max<int64_t>(m, 1),
-                                   0, 64, s);
+    cub::DeviceRadixSort::SortKeys(nullptr, tb_sort, (uint64_t *)nullptr, (uint64_t *)nullptr,
+                                   std::max<int64_t>(std::max(m, n), 1), 0, 64, s);
 
     // carve every buffer up front, with upper bounds, so an oversized graph
     // is refused before anything runs
@@ -940,6 +1408,10 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     int64_t *offp = C.take<int64_t>(n + 1);
     int32_t *adjp = C.take<int32_t>(m + 1);
     int32_t *hubid = C.take<int32_t>(n + 1);
+    int32_t *vrank = C.take<int32_t>(n + 1);
+    int32_t *adjp_rank = C.take<int32_t>(m + 1);
+    uint64_t *rk = C.take<uint64_t>(n + 1);
+    uint64_t *rk2 = C.take<uint64_t>(n + 1);
     uint32_t *tslot = C.take<uint32_t>(nnz + 1);
     uint64_t *keys = C.take<uint64_t>(m + 1);
     uint64_t *keys2 = C.take<uint64_t>(m + 1);
@@ -986,10 +1458,14 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     NA_CUDA(cudaMemsetAsync(flag + nnz, 0, sizeof(uint32_t), s));
     NA_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, nnz + 1, s));
     k_oriented_fill<<<grid_for(std::max(nnz, n + 1)), kThreads, 0, s>>>(d_off, d_adj, flag, pos, n, nnz, offp, adjp);
-    k_hub_flags<<<grid_for(n), kThreads, 0, s>>>(deg, n, flag);
+    k_hub_flags<<<grid_for(n), kThreads, 0, s>>>(deg, n, kCacheHub, flag);
     NA_CUDA(cudaMemsetAsync(flag + n, 0, sizeof(uint32_t), s));
     NA_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, n + 1, s));
     k_hub_ids<<<grid_for(n), kThreads, 0, s>>>(flag, pos, n, hubid);
+    k_rank_keys<<<grid_for(n), kThreads, 0, s>>>(deg, n, rk);
+    NA_CUDA(cub::DeviceRadixSort::SortKeys(tmp, tb, rk, rk2, n, 0, 64, s));
+    k_rank_scatter<<<grid_for(n), kThreads, 0, s>>>(rk2, n, vrank);
+    k_gather_rank<<<grid_for(m), kThreads, 0, s>>>(adjp, vrank, m, adjp_rank);
 
     DevGraph G;
     G.off = d_off;
@@ -1006,6 +1482,12 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     G.m = m;
     G.micro = nullptr;
     G.sums = sums;
+    G.egraph = nullptr;
+    G.gnm = nullptr;
+    G.gdense = nullptr;
+    G.vrank = vrank;
+    G.adjp_rank = adjp_rank;
+    G.anchor_hub = kAnchorHub;
     k_tslot<<<grid_for(32 * m), kThreads, 0, s>>>(G, tslot);
     k_plan_keys<<<grid_for(m), kThreads, 0, s>>>(G, keys, ctr);
     NA_CUDA(cub::DeviceRadixSort::SortKeys(tmp, tb, keys, keys2, m, 0, 64, s));
@@ -1060,5 +1542,220 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     NA_CUDA(cudaStreamSynchronize(s));
     for (int i = 0; i < PGD_NSUMS; i++) out->sums[i] = h[i];
     pgd_close_counts(out->sums, n, m, out->totals);
+    return PGD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched decomposition straight from host pair lists: every graph's pairs
+// are offset into its own vertex range on the device and the whole batch is
+// built as one CSR (one sort), then decomposed with per-graph sums.  Used by
+// the request server, where per-graph set-up would otherwise dominate.
+
+namespace {
+
+__global__ void k_pairs_graph_max(const int64_t *pair_off, int k, const int32_t *src, const int32_t *dst, int64_t P,
+                                  int *gmax, unsigned long long *bad) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P; i += (int64_t)gridDim.x * blockDim.x) {
+        const int g = batch_find(pair_off, k, i);
+        const int32_t a = src[i], b = dst[i];
+        if (a < 0 || b < 0) atomicAdd(bad, 1ull);
+        else if (a != b) atomicMax(gmax + g, max(a, b));
+    }
+}
+
+__global__ void k_pairs_shift(const int64_t *pair_off, int k, const int64_t *vbase, int64_t P, int32_t *src,
+                              int32_t *dst) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P; i += (int64_t)gridDim.x * blockDim.x) {
+        const int g = batch_find(pair_off, k, i);
+        src[i] = (int32_t)(src[i] + vbase[g]);
+        dst[i] = (int32_t)(dst[i] + vbase[g]);
+    }
+}
+
+__global__ void k_vertex_graph(const int64_t *vbase, int k, int64_t N, int32_t *vgraph) {
+    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < N; x += (int64_t)gridDim.x * blockDim.x)
+        vgraph[x] = batch_find(vbase, k, x);
+}
+
+__global__ void k_edge_graph(const int32_t *ev, const int32_t *vgraph, int64_t M, int32_t *egraph) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < M; e += (int64_t)gridDim.x * blockDim.x)
+        egraph[e] = vgraph[ev[e]];
+}
+
+__global__ void k_gather_offsets(const int64_t *off, const int64_t *vbase, int k, int64_t *out) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g <= k; g += (int64_t)gridDim.x * blockDim.x)
+        out[g] = off[vbase[g]];
+}
+
+}  // namespace
+
+pgd_status pgd_dev_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pair_off, const int32_t *src,
+                                         const int32_t *dst, const int64_t *n_min, pgd_counts *out) {
+    cudaStream_t s = ctx->stream;
+    pgd_status st;
+    const int64_t P = pair_off[k];
+    if (P < 0 || P > (int64_t)0x7fffffff) return pgd_fail(ctx, PGD_EINVAL, "pair count out of range");
+    for (int g = 0; g < k; g++)
+        if (pair_off[g + 1] < pair_off[g]) return pgd_fail(ctx, PGD_EINVAL, "pair offsets must not decrease");
+    const int64_t P1 = P > 0 ? P : 1;
+    int32_t *d_src = nullptr, *d_dst = nullptr, *vgraph = nullptr, *egraph = nullptr, *row = nullptr;
+    int64_t *d_poff = nullptr, *d_vbase = nullptr, *d_goff = nullptr, *d_wbase = nullptr;
+    int *gmax = nullptr;
+    uint32_t *flag = nullptr, *pos = nullptr;
+    unsigned long long *gsums = nullptr, *bits = nullptr;
+    long long *d_gnm = nullptr;
+    uint8_t *d_gdense = nullptr;
+    pgd_graph *U = new pgd_graph();
+    U->ctx = ctx;
+    auto cleanup = [&]() {
+        for (void *p : {(void *)d_src, (void *)d_dst, (void *)vgraph, (void *)egraph, (void *)row, (void *)d_poff,
+                        (void *)d_vbase, (void *)d_goff, (void *)d_wbase, (void *)gmax, (void *)flag, (void *)pos,
+                        (void *)gsums, (void *)bits, (void *)d_gnm, (void *)d_gdense})
+            pgd_tmp_free(ctx, p);
+        pgd_graph_destroy(U);
+    };
+#define PB_TRY(expr)                   \
+    do {                               \
+        if ((st = (expr)) != PGD_OK) { \
+            cleanup();                 \
+            return st;                 \
+        }                              \
+    } while (0)
+#define PB_CUDA(call)                                                  \
+    do {                                                               \
+        cudaError_t e__ = (call);                                      \
+        if (e__ != cudaSuccess) {                                      \
+            st = pgd_cuda_fail(ctx, e__, #call);                       \
+            cleanup();                                                 \
+            return st;                                                 \
+        }                                                              \
+    } while (0)
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&d_src, P1 * sizeof(int32_t)));
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&d_dst, P1 * sizeof(int32_t)));
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&d_poff, (k + 1) * sizeof(int64_t)));
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&d_vbase, (k + 1) * sizeof(int64_t)));
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&d_goff, (k + 1) * sizeof(int64_t)));
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&gmax, (size_t)k * sizeof(int)));
+    if (P > 0) {
+        PB_CUDA(cudaMemcpyAsync(d_src, src, P * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        PB_CUDA(cudaMemcpyAsync(d_dst, dst, P * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    }
+    PB_CUDA(cudaMemcpyAsync(d_poff, pair_off, (k + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    PB_CUDA(cudaMemsetAsync(gmax, 0xff, (size_t)k * sizeof(int), s));
+    unsigned long long *bad = ctx->d_ctr + 7;
+    PB_CUDA(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), s));
+    if (P > 0) PGD_LAUNCH(ctx, k_pairs_graph_max, grid_for(P), kThreads, 0, d_poff, k, d_src, d_dst, P, gmax, bad);
+    std::vector<int> hmax((size_t)k);
+    unsigned long long hbad = 0;
+    PB_CUDA(cudaMemcpyAsync(hmax.data(), gmax, (size_t)k * sizeof(int), cudaMemcpyDeviceToHost, s));
+    PB_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(hbad), cudaMemcpyDeviceToHost, s));
+    PB_CUDA(cudaStreamSynchronize(s));
+    if (hbad) {
+        cleanup();
+        return pgd_fail(ctx, PGD_EINVAL, "negative vertex id in a batched edge list");
+    }
+    std::vector<int64_t> vbase((size_t)k + 1, 0);
+    for (int g = 0; g < k; g++) {
+        int64_t ng = std::max<int64_t>(n_min ? n_min[g] : 0, (int64_t)hmax[(size_t)g] + 1);
+        vbase[(size_t)g + 1] = vbase[(size_t)g] + ng;
+    }
+    const int64_t N = vbase[(size_t)k];
+    if (N > 0x7ffffffe) {
+        cleanup();
+        return pgd_fail(ctx, PGD_EINVAL, "batch too large for 32-bit vertex ids");
+    }
+    PB_CUDA(cudaMemcpyAsync(d_vbase, vbase.data(), (k + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    if (P > 0) PGD_LAUNCH(ctx, k_pairs_shift, grid_for(P), kThreads, 0, d_poff, k, d_vbase, P, d_src, d_dst);
+    // one CSR for the whole batch: symmetrised, deduplicated, self loops dropped
+    PB_TRY(pgd_build_from_device_pairs(U, d_src, d_dst, P, N, true));
+    pgd_tmp_free(ctx, d_src);
+    pgd_tmp_free(ctx, d_dst);
+    d_src = d_dst = nullptr;
+    const int64_t M = U->m, nnz = 2 * M;
+    // per-graph edge counts from the offsets at the range boundaries
+    std::vector<int64_t> goff((size_t)k + 1);
+    PGD_LAUNCH(ctx, k_gather_offsets, grid_for(k + 1), kThreads, 0, U->off, d_vbase, k, d_goff);
+    PB_CUDA(cudaMemcpyAsync(goff.data(), d_goff, (k + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    // edge arrays (edge id = position: the order does not change a global count)
+    PB_TRY(pgd_graph_alloc(U, (void **)&U->ev, (M + 1) * sizeof(int32_t)));
+    PB_TRY(pgd_graph_alloc(U, (void **)&U->eu, (M + 1) * sizeof(int32_t)));
+    PB_TRY(pgd_graph_alloc(U, (void **)&U->order, (M + 1) * sizeof(int32_t)));
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&row, (nnz + 1) * sizeof(int32_t)));
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&flag, (nnz + 1) * sizeof(uint32_t)));
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&pos, (nnz + 1) * sizeof(uint32_t)));
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&vgraph, (N + 1) * sizeof(int32_t)));
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&egraph, (M + 1) * sizeof(int32_t)));
+    if (nnz > 0) {
+        PGD_LAUNCH(ctx, k_rows, grid_for(nnz), kThreads, 0, U->off, N, nnz, row);
+        PGD_LAUNCH(ctx, k_na_edge_flags, grid_for(nnz), kThreads, 0, row, U->adj, nnz, flag);
+        PB_CUDA(cudaMemsetAsync(flag + nnz, 0, sizeof(uint32_t), s));
+        size_t tb = 0;
+        void *tmp = nullptr;
+        cub::DeviceScan::ExclusiveSum(nullptr, tb, flag, pos, nnz + 1, s);
+        PB_TRY(pgd_tmp_alloc(ctx, &tmp, tb));
+        cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, nnz + 1, s);
+        pgd_tmp_free(ctx, tmp);
+        PGD_LAUNCH(ctx, k_na_edges, grid_for(nnz), kThreads, 0, row, U->adj, flag, pos, nnz, U->ev, U->eu, U->order);
+    }
+    if (N > 0) PGD_LAUNCH(ctx, k_vertex_graph, grid_for(N), kThreads, 0, d_vbase, k, N, vgraph);
+    if (M > 0) PGD_LAUNCH(ctx, k_edge_graph, grid_for(M), kThreads, 0, U->ev, vgraph, M, egraph);
+    PB_CUDA(cudaStreamSynchronize(s));
+    // per-graph n, m, dense flags
+    std::vector<long long> gnm((size_t)2 * k);
+    std::vector<uint8_t> gdense((size_t)k, 0);
+    std::vector<int64_t> wbase((size_t)k, 0);
+    int64_t words = 0;
+    int ndense_graphs = 0;
+    for (int g = 0; g < k; g++) {
+        const int64_t ng = vbase[(size_t)g + 1] - vbase[(size_t)g];
+        const int64_t mg = (goff[(size_t)g + 1] - goff[(size_t)g]) / 2;
+        gnm[(size_t)2 * g] = ng;
+        gnm[(size_t)2 * g + 1] = mg;
+        if (ng > 0 && ng <= ctx->dense_max && mg > 0) {
+            gdense[(size_t)g] = 1;
+            wbase[(size_t)g] = words;
+            words += ng * ((ng + 63) / 64);
+            ndense_graphs++;
+        }
+    }
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&gsums, (size_t)k * PGD_NSUMS * sizeof(unsigned long long)));
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&d_gnm, gnm.size() * sizeof(long long)));
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&d_gdense, (size_t)k));
+    PB_TRY(pgd_tmp_alloc(ctx, (void **)&d_wbase, (size_t)k * sizeof(int64_t)));
+    if (words > 0) PB_TRY(pgd_tmp_alloc(ctx, (void **)&bits, (size_t)words * sizeof(unsigned long long)));
+    PB_CUDA(cudaMemsetAsync(gsums, 0, (size_t)k * PGD_NSUMS * sizeof(unsigned long long), s));
+    PB_CUDA(cudaMemcpyAsync(d_gnm, gnm.data(), gnm.size() * sizeof(long long), cudaMemcpyHostToDevice, s));
+    PB_CUDA(cudaMemcpyAsync(d_gdense, gdense.data(), (size_t)k, cudaMemcpyHostToDevice, s));
+    PB_CUDA(cudaMemcpyAsync(d_wbase, wbase.data(), (size_t)k * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    if (words > 0) PB_CUDA(cudaMemsetAsync(bits, 0, (size_t)words * sizeof(unsigned long long), s));
+    float ms = 0;
+    if (M > 0) {
+        PB_TRY(build_aux(U));
+        if (words > 0)
+            PGD_LAUNCH(ctx, k_dense_bits, grid_for(32 * N), kThreads, 0, U->off, U->adj, vgraph, d_gdense, d_wbase,
+                       d_vbase, d_gnm, N, bits);
+        DevGraph G = dev_view(U, false);
+        G.sums = gsums;
+        G.egraph = egraph;
+        G.gnm = d_gnm;
+        G.gdense = ndense_graphs ? d_gdense : nullptr;
+        DenseView dv{(const uint64_t *)bits, d_wbase, d_vbase};
+        PB_TRY(run_decompose(ctx, G, U->tslot, U->nhubs, &ms, ndense_graphs ? &dv : nullptr));
+    }
+    std::vector<unsigned long long> h((size_t)k * PGD_NSUMS);
+    PB_CUDA(cudaMemcpyAsync(h.data(), gsums, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    PB_CUDA(cudaStreamSynchronize(s));
+    for (int g = 0; g < k; g++) {
+        pgd_counts &o = out[g];
+        memset(&o, 0, sizeof(o));
+        for (int j = 0; j < PGD_NSUMS; j++) o.sums[j] = h[(size_t)g * PGD_NSUMS + j];
+        o.n = gnm[(size_t)2 * g];
+        o.m = gnm[(size_t)2 * g + 1];
+        o.kernel_ms = ms;
+        pgd_close_counts(o.sums, o.n, o.m, o.totals);
+    }
+    cleanup();
+#undef PB_TRY
+#undef PB_CUDA
     return PGD_OK;
 }

@@ -426,41 +426,50 @@ pgd_status pgd_build_from_pairs(pgd_graph *g, const int32_t *h_src, const int32_
     if (k < 0 || k > (int64_t)0x7fffffff) return pgd_fail(ctx, PGD_EINVAL, "pair count out of range (0..2^31-1)");
     pgd_status st;
     int32_t *d_src = nullptr, *d_dst = nullptr;
-    uint64_t *keys = nullptr, *keys2 = nullptr;
-    uint32_t *vals = nullptr, *vals2 = nullptr;
-    int64_t k1 = k > 0 ? k : 1;
+    const int64_t k1 = k > 0 ? k : 1;
     if ((st = pgd_tmp_alloc(ctx, (void **)&d_src, k1 * sizeof(int32_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&d_dst, k1 * sizeof(int32_t)))) return st;
     if (k > 0) {
         PGD_CUDA(ctx, cudaMemcpyAsync(d_src, h_src, k * sizeof(int32_t), cudaMemcpyHostToDevice, s));
         PGD_CUDA(ctx, cudaMemcpyAsync(d_dst, h_dst, k * sizeof(int32_t), cudaMemcpyHostToDevice, s));
     }
+    st = pgd_build_from_device_pairs(g, d_src, d_dst, k, n_min, dedup);
+    pgd_tmp_free(ctx, d_src);
+    pgd_tmp_free(ctx, d_dst);
+    return st;
+}
+
+pgd_status pgd_build_from_device_pairs(pgd_graph *g, const int32_t *d_src, const int32_t *d_dst, int64_t k,
+                                       int64_t n_min, bool dedup) {
+    pgd_ctx *ctx = g->ctx;
+    cudaStream_t s = ctx->stream;
+    if (k < 0 || k > (int64_t)0x7fffffff) return pgd_fail(ctx, PGD_EINVAL, "pair count out of range (0..2^31-1)");
+    pgd_status st;
+    uint64_t *keys = nullptr, *keys2 = nullptr;
+    uint32_t *vals = nullptr, *vals2 = nullptr;
+    const int64_t k1 = k > 0 ? k : 1;
     // stats: [0] max id (int), [1] self loops, [2] bad ids
     unsigned long long *stats = ctx->d_ctr;
     PGD_CUDA(ctx, cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), s));
     PGD_CUDA(ctx, cudaMemsetAsync(stats, 0xff, sizeof(int), s));  // max id = -1
-    if (k > 0) PGD_LAUNCH(ctx, k_pair_stats, grid_for(k), kThreads, 0, d_src, d_dst, k, (int *)stats, stats + 1, stats + 2);
+    if (k > 0)
+        PGD_LAUNCH(ctx, k_pair_stats, grid_for(k), kThreads, 0, d_src, d_dst, k, (int *)stats, stats + 1, stats + 2);
     unsigned long long h_stats[3];
     PGD_CUDA(ctx, cudaMemcpyAsync(h_stats, stats, sizeof(h_stats), cudaMemcpyDeviceToHost, s));
     PGD_CUDA(ctx, cudaStreamSynchronize(s));
-    int max_id = (int)(h_stats[0] & 0xffffffffu);
-    if (h_stats[2]) {
-        pgd_tmp_free(ctx, d_src); pgd_tmp_free(ctx, d_dst);
-        return pgd_fail(ctx, PGD_EINVAL, "negative vertex id in edge list");
-    }
+    const int max_id = (int)(h_stats[0] & 0xffffffffu);
+    if (h_stats[2]) return pgd_fail(ctx, PGD_EINVAL, "negative vertex id in edge list");
     g->self_loops = (int64_t)h_stats[1];
     g->n = std::max<int64_t>(n_min, (int64_t)max_id + 1);
-    int64_t valid = 2 * (k - g->self_loops);
-    int64_t ne = 2 * k1;
+    const int64_t valid = 2 * (k - g->self_loops);
+    const int64_t ne = 2 * k1;
     if ((st = pgd_tmp_alloc(ctx, (void **)&keys, ne * sizeof(uint64_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&keys2, ne * sizeof(uint64_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&vals, ne * sizeof(uint32_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&vals2, ne * sizeof(uint32_t)))) return st;
-    uint64_t sentinel = (uint64_t)(uint32_t)(max_id + 1) << 32;
+    const uint64_t sentinel = (uint64_t)(uint32_t)(max_id + 1) << 32;
     if (k > 0) PGD_LAUNCH(ctx, k_make_entries, grid_for(k), kThreads, 0, d_src, d_dst, k, sentinel, keys, vals);
-    pgd_tmp_free(ctx, d_src);
-    pgd_tmp_free(ctx, d_dst);
-    int end_bit = 32 + bit_length((uint64_t)(max_id + 1));
+    const int end_bit = 32 + bit_length((uint64_t)(max_id + 1));
     if (k > 0) {
         size_t tb = 0;
         void *tmp = nullptr;

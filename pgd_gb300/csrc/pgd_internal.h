@@ -21,6 +21,10 @@ struct pgd_ctx {
     unsigned long long *d_ctr = nullptr;    // work counters
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     unsigned long long launches = 0;        // kernels of this library launched
+    // decomposition thresholds (results never depend on them; pgd_autotune sets them)
+    int anchor_hub = 128;    // anchors of degree >= this take the bitmap (block) path
+    int cache_hub = 64;      // W(w,p) cached for neighbours of degree >= this
+    int dense_max = 2048;    // batched graphs with at most this many vertices use row bitsets
 };
 
 struct pgd_graph {
@@ -60,6 +64,9 @@ struct pgd_graph {
     int32_t *adjp = nullptr;          // m: neighbours of higher (degree, id)
     int32_t *hubid = nullptr;         // n: slot in the W cache, -1 if none
     int32_t nhubs = 0;
+    int32_t aux_cache_hub = 0;        // cache threshold the hub ids were built with
+    int32_t *vrank = nullptr;         // n: rank by (degree desc, id)
+    int32_t *adjp_rank = nullptr;     // m: vrank of each adjp entry
     uint32_t *tslot = nullptr;        // 2m: triangle count of each slot's edge
 };
 
@@ -91,6 +98,8 @@ void pgd_tmp_free(pgd_ctx *ctx, void *p);
 // Device stages (graph_build.cu).
 pgd_status pgd_build_from_pairs(pgd_graph *g, const int32_t *h_src, const int32_t *h_dst, int64_t k,
                                 int64_t n_min, bool dedup);
+pgd_status pgd_build_from_device_pairs(pgd_graph *g, const int32_t *d_src, const int32_t *d_dst, int64_t k,
+                                       int64_t n_min, bool dedup);
 pgd_status pgd_build_from_csr(pgd_graph *g, const int64_t *h_off, const int32_t *h_adj, int64_t n);
 pgd_status pgd_dev_preprocess(pgd_graph *g, int neigh_kind, int s2l);
 pgd_status pgd_dev_cores(pgd_graph *g);
@@ -99,6 +108,9 @@ pgd_status pgd_dev_sort_edges(pgd_graph *g, int order_kind, int s2l);
 
 // Decomposition (decompose.cu).
 pgd_status pgd_dev_decompose(pgd_graph *g, bool micro, pgd_counts *out);
+pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k, bool micro, pgd_counts *out);
+pgd_status pgd_dev_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pair_off, const int32_t *src,
+                                         const int32_t *dst, const int64_t *n_min, pgd_counts *out);
 
 // Order kinds shared by host parsing and device keys.
 enum pgd_order_kind {

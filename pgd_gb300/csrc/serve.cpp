@@ -1,0 +1,279 @@
+// serve.cpp -- continuous-batching request server (no reference counterpart).
+//
+// Requests (one graph each, as host pairs) are queued on submit.  Each
+// worker thread owns a context (its own CUDA stream) and loops: take the
+// oldest pending requests that fit the server's HBM budget (and at most
+// max_batch of them), decompose them together -- one device CSR for the
+// whole set, one pass of the persistent kernels, per-graph sums
+// (pgd_dev_decompose_pairs_batch) -- publish the results, release the
+// memory.  Requests arriving while a batch is on the GPU are admitted by the
+// next free worker as soon as memory allows, so with two or more workers
+// batches from different workers run on the device at the same time.  A
+// request whose own estimate exceeds the whole budget fails with
+// PGD_ENOMEM; the others are unaffected.
+#include <string.h>
+
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+#include <algorithm>
+
+#include "pgd_internal.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+    uint64_t ticket = 0;
+    std::vector<int32_t> src, dst;
+    int64_t n_min = 0;
+    uint64_t est_bytes = 0;
+    Clock::time_point t_submit, t_done;
+    pgd_counts result{};
+    pgd_status status = PGD_OK;
+    bool done = false;
+};
+
+// Device bytes one request needs while it is decomposed: pairs and their
+// sort buffers, the CSR with its per-slot arrays, per-edge and per-vertex
+// work arrays.  Deliberately generous; only used for admission.
+uint64_t estimate_bytes(int64_t pairs, int64_t n) {
+    const uint64_t p = (uint64_t)std::max<int64_t>(pairs, 1), v = (uint64_t)std::max<int64_t>(n, 1);
+    return 160 * p + 64 * v + (64u << 10);
+}
+
+}  // namespace
+
+struct pgd_server {
+    pgd_server_opts opts{};
+    std::vector<pgd_ctx *> ctxs;
+    std::vector<std::thread> workers;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Request *> pending;
+    std::unordered_map<uint64_t, Request *> requests;
+    uint64_t next_ticket = 1, inflight = 0, peak = 0;
+    uint64_t submitted = 0, completed = 0, rejected = 0, batches = 0;
+    std::vector<double> latencies_ms;
+    Clock::time_point t_first{}, t_last{};
+    bool have_first = false;
+    bool stop = false;
+
+    void run(int wi) {
+        pgd_ctx *ctx = ctxs[(size_t)wi];
+        std::vector<Request *> batch;
+        std::vector<int64_t> off, nmin;
+        std::vector<int32_t> src, dst;
+        std::vector<pgd_counts> out;
+        while (true) {
+            batch.clear();
+            uint64_t bytes = 0;
+            {
+                std::unique_lock<std::mutex> lock(mu);
+                cv_work.wait(lock, [&] { return stop || !pending.empty(); });
+                if (pending.empty() && stop) return;
+                // admit the oldest requests that fit; refuse what can never fit
+                while (!pending.empty() && (int)batch.size() < opts.max_batch) {
+                    Request *r = pending.front();
+                    if (r->est_bytes > opts.hbm_budget) {
+                        pending.pop_front();
+                        r->status = PGD_ENOMEM;
+                        r->done = true;
+                        r->t_done = Clock::now();
+                        rejected++;
+                        cv_done.notify_all();
+                        continue;
+                    }
+                    if (inflight + bytes + r->est_bytes > opts.hbm_budget) break;
+                    pending.pop_front();
+                    bytes += r->est_bytes;
+                    batch.push_back(r);
+                }
+                if (batch.empty()) {
+                    // everything left waits for memory held by other workers
+                    cv_work.wait_for(lock, std::chrono::milliseconds(1));
+                    continue;
+                }
+                inflight += bytes;
+                peak = std::max(peak, inflight);
+                batches++;
+            }
+            off.assign(1, 0);
+            nmin.clear();
+            src.clear();
+            dst.clear();
+            for (Request *r : batch) {
+                src.insert(src.end(), r->src.begin(), r->src.end());
+                dst.insert(dst.end(), r->dst.begin(), r->dst.end());
+                off.push_back((int64_t)src.size());
+                nmin.push_back(r->n_min);
+            }
+            out.assign(batch.size(), pgd_counts{});
+            pgd_status st = pgd_dev_decompose_pairs_batch(ctx, (int)batch.size(), off.data(), src.data(), dst.data(),
+                                                          nmin.data(), out.data());
+            const Clock::time_point now = Clock::now();
+            {
+                std::lock_guard<std::mutex> lock(mu);
+                for (size_t i = 0; i < batch.size(); i++) {
+                    Request *r = batch[i];
+                    r->status = st;
+                    if (st == PGD_OK) r->result = out[i];
+                    r->done = true;
+                    r->t_done = now;
+                    r->src.clear();
+                    r->src.shrink_to_fit();
+                    r->dst.clear();
+                    r->dst.shrink_to_fit();
+                    completed++;
+                    latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
+                }
+                t_last = now;
+                inflight -= bytes;
+            }
+            cv_done.notify_all();
+            cv_work.notify_all();
+        }
+    }
+};
+
+extern "C" pgd_status pgd_server_create(const pgd_server_opts *opts, pgd_server **out) {
+    if (!out) return PGD_EINVAL;
+    *out = nullptr;
+    pgd_server *sv = new pgd_server();
+    if (opts) sv->opts = *opts;
+    if (sv->opts.workers <= 0) sv->opts.workers = 2;
+    if (sv->opts.max_batch <= 0) sv->opts.max_batch = 4096;
+    for (int i = 0; i < sv->opts.workers; i++) {
+        pgd_opts o{};
+        o.device = sv->opts.device;
+        pgd_ctx *c = nullptr;
+        pgd_status st = pgd_context_create(&o, &c);
+        if (st) {
+            for (pgd_ctx *x : sv->ctxs) pgd_context_destroy(x);
+            delete sv;
+            return st;
+        }
+        sv->ctxs.push_back(c);
+    }
+    if (!sv->opts.hbm_budget) sv->opts.hbm_budget = sv->ctxs[0]->budget / 2;
+    for (pgd_ctx *c : sv->ctxs) c->budget = UINT64_MAX;  // admission is the server's job
+    for (int i = 0; i < sv->opts.workers; i++) sv->workers.emplace_back([sv, i] { sv->run(i); });
+    *out = sv;
+    return PGD_OK;
+}
+
+extern "C" pgd_status pgd_server_submit(pgd_server *sv, const int32_t *src, const int32_t *dst, int64_t k,
+                                        int64_t n_min, uint64_t *ticket) {
+    if (!sv || !ticket || k < 0 || (k > 0 && (!src || !dst)) || n_min < 0) return PGD_EINVAL;
+    Request *r = new Request();
+    r->src.assign(src, src + k);
+    r->dst.assign(dst, dst + k);
+    r->n_min = n_min;
+    int64_t n = n_min;
+    for (int64_t i = 0; i < k; i++) n = std::max<int64_t>(n, (int64_t)std::max(src[i], dst[i]) + 1);
+    r->est_bytes = estimate_bytes(k, n);
+    r->t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> lock(sv->mu);
+        if (sv->stop) {
+            delete r;
+            return PGD_EINVAL;
+        }
+        r->ticket = sv->next_ticket++;
+        sv->requests[r->ticket] = r;
+        sv->pending.push_back(r);
+        sv->submitted++;
+        if (!sv->have_first) {
+            sv->t_first = r->t_submit;
+            sv->have_first = true;
+        }
+    }
+    sv->cv_work.notify_one();
+    *ticket = r->ticket;
+    return PGD_OK;
+}
+
+static pgd_status take_result(pgd_server *sv, std::unordered_map<uint64_t, Request *>::iterator it, pgd_counts *out) {
+    Request *r = it->second;
+    pgd_status st = r->status;
+    if (out) *out = r->result;
+    sv->requests.erase(it);
+    delete r;
+    return st;
+}
+
+extern "C" pgd_status pgd_server_poll(pgd_server *sv, uint64_t ticket, pgd_counts *out, int *done) {
+    if (!sv || !done) return PGD_EINVAL;
+    std::lock_guard<std::mutex> lock(sv->mu);
+    auto it = sv->requests.find(ticket);
+    if (it == sv->requests.end()) return PGD_EINVAL;
+    *done = it->second->done ? 1 : 0;
+    if (!*done) return PGD_OK;
+    return take_result(sv, it, out);
+}
+
+extern "C" pgd_status pgd_server_wait(pgd_server *sv, uint64_t ticket, int timeout_ms, pgd_counts *out) {
+    if (!sv) return PGD_EINVAL;
+    std::unique_lock<std::mutex> lock(sv->mu);
+    auto it = sv->requests.find(ticket);
+    if (it == sv->requests.end()) return PGD_EINVAL;
+    Request *r = it->second;
+    if (!sv->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms),
+                              [&] { return r->done; }))
+        return PGD_ETIMEOUT;
+    return take_result(sv, sv->requests.find(ticket), out);
+}
+
+extern "C" pgd_status pgd_server_stats(pgd_server *sv, pgd_server_stat *st) {
+    if (!sv || !st) return PGD_EINVAL;
+    std::lock_guard<std::mutex> lock(sv->mu);
+    memset(st, 0, sizeof(*st));
+    st->submitted = sv->submitted;
+    st->completed = sv->completed;
+    st->rejected = sv->rejected;
+    st->batches = sv->batches;
+    st->inflight_bytes = sv->inflight;
+    st->peak_bytes = sv->peak;
+    std::vector<double> l = sv->latencies_ms;
+    if (!l.empty()) {
+        std::sort(l.begin(), l.end());
+        auto q = [&](double f) { return l[std::min(l.size() - 1, (size_t)(f * (double)(l.size() - 1) + 0.5))]; };
+        st->p50_ms = q(0.50);
+        st->p99_ms = q(0.99);
+        double s = 0;
+        for (double x : l) s += x;
+        st->mean_ms = s / (double)l.size();
+        const double span = std::chrono::duration<double>(sv->t_last - sv->t_first).count();
+        st->graphs_per_s = span > 0 ? (double)sv->completed / span : 0;
+    }
+    return PGD_OK;
+}
+
+extern "C" pgd_status pgd_server_destroy(pgd_server *sv) {
+    if (!sv) return PGD_EINVAL;
+    {
+        std::lock_guard<std::mutex> lock(sv->mu);
+        sv->stop = true;
+    }
+    sv->cv_work.notify_all();
+    for (std::thread &t : sv->workers) t.join();
+    for (auto &kv : sv->requests) delete kv.second;
+    for (pgd_ctx *c : sv->ctxs) pgd_context_destroy(c);
+    delete sv;
+    return PGD_OK;
+}
+
+extern "C" pgd_status pgd_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pair_off, const int32_t *src,
+                                                const int32_t *dst, const int64_t *n_min, pgd_counts *out) {
+    if (!ctx || k < 0 || (k > 0 && (!pair_off || !out)) || (k > 0 && pair_off[k] > 0 && (!src || !dst)))
+        return pgd_fail(ctx, PGD_EINVAL, "bad arguments");
+    if (k == 0) return PGD_OK;
+    cudaSetDevice(ctx->device);
+    return pgd_dev_decompose_pairs_batch(ctx, k, pair_off, src, dst, n_min, out);
+}

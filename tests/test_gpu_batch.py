@@ -1,0 +1,88 @@
+"""Batched decomposition (many uneven graphs in one pass) and the work-split
+thresholds: per-graph results identical to single-graph decomposition and to
+the oracle, whatever the thresholds."""
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+import pgd_gb300 as pgd
+
+pytestmark = pytest.mark.gpu
+
+
+def mixed_graphs(count, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = int(rng.integers(16, 400))
+        kind = i % 4
+        if kind == 0:
+            out.append(pgd.erdos_renyi(n, float(rng.uniform(0.01, 0.5)), seed=seed * 1000 + i))
+        elif kind == 1:
+            out.append(pgd.barabasi_albert(n, int(rng.integers(2, 9)), seed=seed * 1000 + i))
+        elif kind == 2:
+            out.append(pgd.rmat(int(rng.integers(6, 10)), 8, seed=seed * 1000 + i))
+        else:
+            k = int(rng.integers(0, 3 * n))
+            out.append((rng.integers(0, n, k).astype(np.int32), rng.integers(0, n, k).astype(np.int32)))
+    return out
+
+
+@pytest.mark.parametrize("dense_max", [0, 128, 2048])
+def test_batch_matches_single_and_oracle(dense_max):
+    ctx = pgd.Context()
+    ctx.set_thresholds(128, 64, dense_max)
+    pairs = mixed_graphs(40, 1) + [(np.zeros(0, np.int32), np.zeros(0, np.int32)),
+                                   (np.array([0], np.int32), np.array([1], np.int32))]
+    graphs = [ctx.graph_from_edges(s, d) for s, d in pairs]
+    for i, g in enumerate(graphs):
+        g.preprocess("deg")
+        g.sort_edges("kcore" if i % 2 else "deg")
+    res = ctx.decompose_batch(graphs, micro=True)
+    for i, ((s, d), g, r) in enumerate(zip(pairs, graphs, res)):
+        o = ol.OracleGraph.from_pairs(s, d, dedup=True).run(order="kcore" if i % 2 else "deg")
+        assert (r.totals == o.totals()).all(), i
+        assert (r.sums == o.sums()).all(), i
+        a, b, c = g.micro()
+        x, y, z = o.micro()
+        assert (a == x).all() and (b == y).all() and (c == z).all(), i
+        single = g.decompose(micro=False)
+        assert (single.totals == r.totals).all()
+    ctx.close()
+
+
+@pytest.mark.parametrize("anchor,cache", [(2, 2), (32, 512), (256, 32), (64, 64), (128, 1 << 30)])
+def test_thresholds_never_change_counts(anchor, cache):
+    c = pgd.Context()
+    c.set_thresholds(anchor, cache)
+    assert c.thresholds() == (anchor, cache, 2048)
+    for s, d in [pgd.rmat(12, 16, seed=3), pgd.erdos_renyi(300, 0.3, seed=4), pgd.barabasi_albert(2000, 7, seed=5)]:
+        g = c.graph_from_edges(s, d)
+        r = g.decompose(micro=True)
+        o = ol.OracleGraph.from_pairs(s, d, dedup=True).run()
+        assert (r.totals == o.totals()).all()
+        assert (g.micro()[2] == o.micro()[2]).all()
+    c.close()
+
+
+def test_thresholds_rejected_out_of_range(ctx):
+    with pytest.raises(pgd.PGDError):
+        ctx.set_thresholds(1, 64)
+    with pytest.raises(pgd.PGDError):
+        ctx.set_thresholds(300, 64)
+    with pytest.raises(pgd.PGDError):
+        ctx.set_thresholds(128, 64, 4096)
+
+
+def test_autotune_keeps_counts():
+    c = pgd.Context()
+    pairs = mixed_graphs(12, 7)
+    graphs = [c.graph_from_edges(s, d) for s, d in pairs]
+    a, h, d, ms = c.autotune(graphs, reps=1)
+    assert 2 <= a <= 256 and h >= 2 and 0 <= d <= 2048 and ms > 0
+    assert c.thresholds() == (a, h, d)
+    res = c.decompose_batch(graphs)
+    for (s, d), r in zip(pairs, res):
+        o = ol.OracleGraph.from_pairs(s, d, dedup=True).run(micro=False)
+        assert (r.totals == o.totals()).all()
+    c.close()

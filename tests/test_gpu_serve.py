@@ -1,0 +1,105 @@
+"""Batched decomposition from host pair lists and the continuous-batching
+request server: every request's counts equal the oracle's for that graph
+alone, under concurrency, memory refusal and timeouts."""
+import threading
+
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+import pgd_gb300 as pgd
+
+pytestmark = pytest.mark.gpu
+
+
+def request_mix(count, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        kind = i % 5
+        if kind == 0:
+            out.append(pgd.rmat(int(rng.integers(5, 11)), 8, seed=seed * 100 + i))
+        elif kind == 1:
+            out.append(pgd.erdos_renyi(int(rng.integers(10, 300)), float(rng.uniform(0.02, 0.5)), seed=seed * 100 + i))
+        elif kind == 2:
+            out.append(pgd.barabasi_albert(int(rng.integers(10, 1500)), int(rng.integers(2, 8)), seed=seed * 100 + i))
+        elif kind == 3:
+            n = int(rng.integers(2, 80))
+            k = int(rng.integers(0, 4 * n))
+            out.append((rng.integers(0, n, k).astype(np.int32), rng.integers(0, n, k).astype(np.int32)))
+        else:
+            out.append((np.zeros(0, np.int32), np.zeros(0, np.int32)))
+    return out
+
+
+def oracle_totals(s, d, n_min=0):
+    return ol.OracleGraph.from_pairs(s, d, n_min=n_min, dedup=True).run(micro=False).totals()
+
+
+@pytest.mark.parametrize("dense_max", [0, 2048])
+def test_pairs_batch_matches_oracle(dense_max):
+    ctx = pgd.Context()
+    ctx.set_thresholds(128, 64, dense_max)
+    graphs = request_mix(60, 3)
+    n_min = [0] * len(graphs)
+    n_min[3] = 500  # isolated vertices count in n
+    res = ctx.decompose_pairs_batch(graphs, n_min=n_min)
+    for i, ((s, d), r) in enumerate(zip(graphs, res)):
+        assert (r.totals == oracle_totals(s, d, n_min[i])).all(), i
+    ctx.close()
+
+
+def test_server_results_and_stats():
+    sv = pgd.Server(workers=2)
+    graphs = request_mix(80, 5)
+    tickets = [None] * len(graphs)
+
+    def submit(lo, hi):
+        for i in range(lo, hi):
+            tickets[i] = sv.submit(*graphs[i])
+
+    threads = [threading.Thread(target=submit, args=(j * 20, (j + 1) * 20)) for j in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for i, tk in enumerate(tickets):
+        st, r = sv.wait(tk, 120000)
+        assert st == 0
+        assert (r.totals == oracle_totals(*graphs[i])).all(), i
+    s = sv.stats()
+    assert s["completed"] == len(graphs) and s["rejected"] == 0
+    assert s["batches"] >= 1 and s["p99_ms"] >= s["p50_ms"] > 0 and s["graphs_per_s"] > 0
+    sv.close()
+
+
+def test_server_refuses_what_cannot_fit():
+    sv = pgd.Server(workers=1, hbm_budget=4 << 20)
+    big = pgd.rmat(14, 16, seed=1)           # estimate far above 4 MiB
+    small = pgd.erdos_renyi(40, 0.3, seed=2)
+    tb = sv.submit(*big)
+    ts = sv.submit(*small)
+    st, _ = sv.wait(tb, 60000)
+    assert st == 2  # PGD_ENOMEM
+    st, r = sv.wait(ts, 60000)
+    assert st == 0 and (r.totals == oracle_totals(*small)).all()
+    assert sv.stats()["rejected"] == 1
+    sv.close()
+
+
+def test_server_poll_and_timeout():
+    sv = pgd.Server(workers=1)
+    s, d = pgd.rmat(12, 16, seed=9)
+    t = sv.submit(s, d)
+    st, _ = sv.wait(t, 0)
+    assert st in (0, 3)  # done already, or PGD_ETIMEOUT with the request still running
+    if st == 3:
+        got = None
+        for _ in range(10000):
+            got = sv.poll(t)
+            if got is not None:
+                break
+            threading.Event().wait(0.005)
+        assert got is not None and got[0] == 0
+        assert (got[1].totals == oracle_totals(s, d)).all()
+    sv.close()
