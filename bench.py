@@ -35,9 +35,9 @@ METRIC = "edges/s full 4-node counts (bit-exact)"
 UNIT = "edges/s"
 RMAT = dict(a=0.57, b=0.19, c=0.19)
 
-# DRAM traffic of one k_decompose launch on this workload, from the ncu
-# capture summarised in profiles/ (None until a capture exists).
-NCU_TRAFFIC_BYTES = None
+# DRAM traffic (read + write) of one k_hub launch, the dominant kernel, on
+# this workload: a full-size single-pass ncu capture, profiles/k_hub_rmat20_dram.md.
+NCU_TRAFFIC_BYTES = 2427096476928 + 25345573632
 
 
 def log(*a):
@@ -301,7 +301,8 @@ def main():
     peak, peak_src = peaks()
     achieved = b_alg / kern_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": NCU_TRAFFIC_BYTES, "kernel": "k_decompose", "kernel_ms": float(np.mean(kernel_ms)),
+                "traffic": NCU_TRAFFIC_BYTES if args.scale == 20 and args.order == "kcore" else None,
+                "kernel": "k_hub (97 % of the decomposition kernels' time)", "kernel_ms": float(np.mean(kernel_ms)),
                 "algorithmic_bytes": b_alg, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)"
                 if peak_src == "measured" else "fallback 6.8 TB/s"}
 

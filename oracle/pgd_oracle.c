@@ -847,6 +847,46 @@ int64_t po_decompose_sample(po_graph *g, int threads, int cheap_side, int64_t st
     return ne;
 }
 
+int po_edge_sample(po_graph *g, int64_t k, const int64_t *vs, const int64_t *us, uint64_t *tout, uint64_t *k4out,
+                   uint64_t *c4out, int threads) {
+    int64_t n = g->n;
+    for (int64_t i = 0; i < k; i++)
+        if (vs[i] < 0 || vs[i] >= n || us[i] < 0 || us[i] >= n) return -1;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+#pragma omp parallel
+    {
+        uint8_t *ind = calloc((size_t)n + 1, 1);
+        int32_t *T = malloc((size_t)(g->max_degree + 1) * sizeof(int32_t));
+        int32_t *S = malloc((size_t)(g->max_degree + 1) * sizeof(int32_t));
+#pragma omp for schedule(dynamic, 1)
+        for (int64_t i = 0; i < k; i++) {
+            long long v = vs[i], u = us[i];
+            for (int64_t j = g->off[v]; j < g->off[v + 1]; j++) if (g->adj[j] != u) ind[g->adj[j]] = 1;
+            ull t = 0, ns = 0, c4 = 0, k4 = 0;
+            for (int64_t j = g->off[u]; j < g->off[u + 1]; j++) {
+                int32_t w = g->adj[j];
+                if (w == v) continue;
+                if (ind[w] == 1) { ind[w] = 3; T[t++] = w; }
+                else S[ns++] = w;
+            }
+            for (ull a = 0; a < ns; a++)
+                for (int64_t j = g->off[S[a]]; j < g->off[S[a] + 1]; j++) c4 += (ind[g->adj[j]] == 1);
+            for (ull a = 0; a < t; a++) {
+                for (int64_t j = g->off[T[a]]; j < g->off[T[a] + 1]; j++) k4 += (ind[g->adj[j]] == 3);
+                ind[T[a]] = 0;
+            }
+            for (int64_t j = g->off[v]; j < g->off[v + 1]; j++) ind[g->adj[j]] = 0;
+            tout[i] = t;
+            k4out[i] = k4;
+            c4out[i] = c4;
+        }
+        free(ind); free(T); free(S);
+    }
+    return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 int64_t po_n(const po_graph *g) { return g->n; }
 int64_t po_m(const po_graph *g) { return g->m; }

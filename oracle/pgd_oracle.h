@@ -60,6 +60,13 @@ int po_decompose(po_graph *g, int micro, int threads, int cheap_side);
  * wall time of the loop alone.  Results are not kept. */
 int64_t po_decompose_sample(po_graph *g, int threads, int cheap_side, int64_t stride, double *seconds);
 
+/* t, k4, c4 of the edges (vs[i], us[i]), each by the reference's own
+ * marking procedure (graphlet_core.cpp:1069-1240: mark N(v), scan N(u));
+ * for checking sampled rows of graphs too large for a full oracle run.
+ * Needs only the CSR. */
+int po_edge_sample(po_graph *g, int64_t k, const int64_t *vs, const int64_t *us, uint64_t *t, uint64_t *k4,
+                   uint64_t *c4, int threads);
+
 /* Closing identities (graphlet_core.cpp:1449-1472, graphlet_core.h:548-557). */
 void po_close(const uint64_t sums[PO_NSUMS], int64_t n, int64_t m, uint64_t totals[PO_NTOTALS]);
 

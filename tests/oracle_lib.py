@@ -59,6 +59,7 @@ def lib():
         L.po_sort_edges.argtypes = [_P, ctypes.c_char_p, ctypes.c_int]
         L.po_decompose.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.po_close.argtypes = [_U64P, ctypes.c_int64, ctypes.c_int64, _U64P]
+        L.po_edge_sample.argtypes = [_P, ctypes.c_int64, _I64P, _I64P, _U64P, _U64P, _U64P, ctypes.c_int]
         L.po_decompose_sample.restype = ctypes.c_int64
         L.po_decompose_sample.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int64,
                                           ctypes.POINTER(ctypes.c_double)]
@@ -148,6 +149,15 @@ class OracleGraph:
         sec = ctypes.c_double()
         k = lib().po_decompose_sample(self.h, threads, int(cheap_side), stride, ctypes.byref(sec))
         return k, sec.value
+
+    def edge_sample(self, vs, us, threads=0):
+        """(t, k4, c4) of the edges (vs[i], us[i]) by the reference's marking procedure"""
+        vs = np.ascontiguousarray(vs, np.int64)
+        us = np.ascontiguousarray(us, np.int64)
+        t, k, c = (np.zeros(max(1, len(vs)), np.uint64) for _ in range(3))
+        if lib().po_edge_sample(self.h, len(vs), vs, us, t, k, c, threads):
+            raise ValueError("vertex id out of range")
+        return t[: len(vs)], k[: len(vs)], c[: len(vs)]
 
     def csr(self):
         off = np.zeros(self.n + 1, np.int64)
