@@ -1,7 +1,9 @@
 """Benchmarks of the batched and served decomposition paths.
 
     python -m pgd_gb300.benchmarks batch [--graphs 4096] [--seed 1]
-    python -m pgd_gb300.benchmarks serve [--requests 2000] [--rate 2000] [--seed 1]
+    python -m pgd_gb300.benchmarks serve [--requests 2000] [--rate 4000 | --rates 1000,4000,...] [--seed 1]
+    python -m pgd_gb300.benchmarks large [--workloads rmat24,rgg24] [--samples 1000]
+    python -m pgd_gb300.benchmarks profile [--scale 18] [--order kcore] [--reps 1]
 
 batch: 4096 independent graphs, n uniform in [16, 2048]; half G(n, p) with p
 uniform in [0.01, 0.5], half Barabasi-Albert with m uniform in {2..8}; all
@@ -14,11 +16,24 @@ serve: requests arrive as a Poisson process of `rate` per second; each
 request's edge count is lognormal (median 5000, sigma 1.2, clipped at 50 M),
 half RMAT (scale ceil(log2(m/16)), edge factor chosen to hit m) and half
 G(n, p) with mean degree 16.  They go to the continuous-batching server;
-reported: graphs/s, p50/p99 latency (submit to result), and the same
-request list through the plain one-graph-per-call loop.
+reported per offered rate: graphs/s, p50/p99 latency (submit to result),
+and the same request list through the plain one-graph-per-call loop.
 
-Every result is checked against the plain path's counts.  Prints one JSON
-line per mode.
+large: RMAT scale 24 (edge factor 16, (a,b,c,d) = (0.57,0.19,0.19,0.05),
+seed 1) and the 3-D random geometric graph with n = 2^24 in the unit cube,
+radius (3*24 / (4 pi n))^(1/3) (seed 1), each with degeneracy order and
+per-edge counts.  Timed: sort_edges + decomposition of the resident graph
+(the reference's "graphlet decomposition time"); the CSR build is reported
+separately.  Checked: the per-edge columns against the global sums, the
+closing identities, and a seeded random sample of rows plus the heaviest rows
+against the oracle's marking procedure on those edges.
+
+profile: one RMAT graph of the given scale, k-core order, decomposed `reps`
+times with per-edge counts; prints the kernel time of each run.  This is the
+command the ncu captures of the decomposition kernels are taken on.
+
+Every batch/serve result is checked against the plain path's counts.  Prints
+one JSON line per mode (per workload for `large`).
 """
 import argparse
 import concurrent.futures as cf
@@ -131,25 +146,9 @@ def serve_requests(count, seed):
         return list(ex.map(make, specs))
 
 
-def run_serve(args):
-    t0 = time.perf_counter()
-    reqs = serve_requests(args.requests, args.seed)
-    pairs = sum(len(s) for s, _ in reqs)
-    log("generated %d requests, %d pairs in %.1fs" % (len(reqs), pairs, time.perf_counter() - t0))
-    rng = np.random.default_rng(args.seed + 1)
-    gaps = rng.exponential(1.0 / args.rate, len(reqs))
-    # plain loop first (also the expected counts)
-    ctx = pgd.Context()
-    plain_loop(ctx, reqs[:16])
-    expect, plain_s = plain_loop(ctx, reqs)
-    ctx.close()
-    log("plain loop: %.1f graphs/s" % (len(reqs) / plain_s))
-    sv = pgd.Server(workers=args.workers)
-    # warm-up
-    for s, d in reqs[:8]:
-        sv.wait(sv.submit(s, d), 60000)
-    sv.close()
-    sv = pgd.Server(workers=args.workers)
+def serve_once(reqs, expect, gaps, workers):
+    """Submit reqs on the Poisson schedule gaps; wait for all; check them."""
+    sv = pgd.Server(workers=workers)
     tickets = []
     t_start = time.perf_counter()
     next_t = t_start
@@ -168,34 +167,149 @@ def run_serve(args):
     wall = time.perf_counter() - t_start
     stats = sv.stats()
     sv.close()
-    line = {
-        "mode": "serve", "requests": len(reqs), "pairs": pairs, "offered_rate": args.rate,
-        "graphs_per_s": stats["graphs_per_s"], "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"],
-        "mean_ms": stats["mean_ms"], "batches": stats["batches"], "wall_s": wall,
-        "plain_graphs_per_s": len(reqs) / plain_s,
-        "speedup_vs_plain": stats["graphs_per_s"] / (len(reqs) / plain_s), "mismatches_vs_plain": mismatch,
-        "workers": args.workers,
-        "workload": "Poisson arrivals; m ~ lognormal(median 5000, sigma 1.2, <= 50M); half RMAT, half G(n,p) "
-                    "mean degree 16; seed %d" % args.seed,
-    }
-    print(json.dumps(line), flush=True)
+    return stats, wall, mismatch
+
+
+def run_serve(args):
+    t0 = time.perf_counter()
+    reqs = serve_requests(args.requests, args.seed)
+    pairs = sum(len(s) for s, _ in reqs)
+    log("generated %d requests, %d pairs in %.1fs" % (len(reqs), pairs, time.perf_counter() - t0))
+    # plain loop first (also the expected counts)
+    ctx = pgd.Context()
+    plain_loop(ctx, reqs[:16])
+    expect, plain_s = plain_loop(ctx, reqs)
+    ctx.close()
+    plain_rate = len(reqs) / plain_s
+    log("plain loop: %.1f graphs/s" % plain_rate)
+    # warm-up
+    sv = pgd.Server(workers=args.workers)
+    for s, d in reqs[:8]:
+        sv.wait(sv.submit(s, d), 60000)
+    sv.close()
+    rates = [float(r) for r in args.rates.split(",")] if args.rates else [args.rate]
+    for rate in rates:
+        rng = np.random.default_rng(args.seed + 1)
+        gaps = rng.exponential(1.0 / rate, len(reqs))
+        stats, wall, mismatch = serve_once(reqs, expect, gaps, args.workers)
+        line = {
+            "mode": "serve", "requests": len(reqs), "pairs": pairs, "offered_rate": rate,
+            "graphs_per_s": stats["graphs_per_s"], "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"],
+            "mean_ms": stats["mean_ms"], "batches": stats["batches"], "wall_s": wall,
+            "plain_graphs_per_s": plain_rate, "speedup_vs_plain": stats["graphs_per_s"] / plain_rate,
+            "mismatches_vs_plain": mismatch, "workers": args.workers,
+            "workload": "Poisson arrivals; m ~ lognormal(median 5000, sigma 1.2, <= 50M); half RMAT, half G(n,p) "
+                        "mean degree 16; seed %d" % args.seed,
+        }
+        print(json.dumps(line), flush=True)
+
+
+RMAT = dict(a=0.57, b=0.19, c=0.19)
+
+
+def run_profile(args):
+    s, d = pgd.rmat(args.scale, 16, seed=1, **RMAT)
+    ctx = pgd.Context()
+    g = ctx.graph_from_edges(s, d)
+    g.preprocess("deg")
+    g.compute_cores()
+    g.sort_edges(args.order)
+    for _ in range(args.reps):
+        res = g.decompose(micro=True)
+        print(json.dumps({"mode": "profile", "scale": args.scale, "order": args.order, "n": int(res.n),
+                          "m": int(res.m), "kernel_ms": float(res.kernel_ms)}), flush=True)
+
+
+def large_pairs(name, seed):
+    if name == "rmat24":
+        return pgd.rmat(24, 16, seed=seed, **RMAT), "RMAT scale 24, edge factor 16, (0.57,0.19,0.19,0.05)"
+    if name == "rgg24":
+        n = 1 << 24
+        r = (3 * 24 / (4 * math.pi * n)) ** (1.0 / 3.0)
+        return pgd.rgg3d(n, r, seed=seed), "3-D RGG n=2^24 in the unit cube, r=%.6f" % r
+    raise ValueError(name)
+
+
+def run_large(args):
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests"))
+    for name in args.workloads.split(","):
+        t0 = time.perf_counter()
+        (src, dst), desc = large_pairs(name, args.seed)
+        gen_s = time.perf_counter() - t0
+        ctx = pgd.Context()
+        t0 = time.perf_counter()
+        g = ctx.graph_from_edges(src, dst)
+        g.preprocess("deg")
+        g.compute_cores()
+        build_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        g.sort_edges("kcore")
+        res = g.decompose(micro=True)
+        step_s = time.perf_counter() - t0
+        m = int(res.m)
+        log("%s: n=%d m=%d build %.1fs, sort+decompose %.2fs (kernels %.1f ms)"
+            % (name, res.n, m, build_s, step_s, res.kernel_ms))
+        s1, d1, cols = g.micro()
+        M64 = (1 << 64) - 1
+        tot = dict(zip(pgd.TOTAL_NAMES, (int(x) for x in res.totals)))
+        N = {i: int(res.sums[4 + i]) for i in range(1, 11)}
+        checks = {
+            "sum_t": bool(res.sums[0] == cols[:, 0].sum(dtype=np.uint64)),
+            "sum_k4": bool(res.sums[3] == cols[:, 2].sum(dtype=np.uint64)),
+            "sum_c4": bool(res.sums[4] == cols[:, 5].sum(dtype=np.uint64)),
+            "chord_clique": (tot["total_4_chordcycle"] + 6 * tot["total_4_clique"]) & M64 == N[3],
+            "path_cycle": (tot["total_4_path"] + 4 * tot["total_4_cycle"]) & M64 == N[5],
+        }
+        # sampled rows against the oracle (host CSR of the same pairs)
+        import oracle_lib as ol
+
+        t0 = time.perf_counter()
+        o = ol.OracleGraph.from_pairs(src, dst, dedup=True)
+        rng = np.random.default_rng(args.seed)
+        pos = np.concatenate([rng.choice(m, size=min(args.samples, m), replace=False),
+                              np.arange(min(args.heavy, m))])
+        t_o, k_o, c_o = o.edge_sample(s1[pos] - 1, d1[pos] - 1)
+        checks["sampled_rows"] = int(len(pos))
+        checks["sampled_rows_equal"] = bool((t_o == cols[pos, 0]).all() and (k_o == cols[pos, 2]).all()
+                                            and (c_o == cols[pos, 5]).all())
+        oracle_s = time.perf_counter() - t0
+        line = {
+            "mode": "large", "workload": name, "graph": desc, "n": int(res.n), "m": m,
+            "edges_per_s": m / step_s, "seconds": step_s, "kernel_ms": float(res.kernel_ms),
+            "build_seconds": build_s, "generate_seconds": gen_s, "oracle_check_seconds": oracle_s,
+            "checks": checks, "totals": tot,
+        }
+        print(json.dumps(line), flush=True)
+        del o, cols, s1, d1
+        g.destroy()
+        ctx.close()
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("mode", choices=["batch", "serve"])
+    ap.add_argument("mode", choices=["batch", "serve", "large", "profile"])
+    ap.add_argument("--workloads", default="rmat24,rgg24")
+    ap.add_argument("--samples", type=int, default=1000)
+    ap.add_argument("--heavy", type=int, default=10)
+    ap.add_argument("--scale", type=int, default=18)
+    ap.add_argument("--order", default="kcore")
     ap.add_argument("--graphs", type=int, default=4096)
     ap.add_argument("--requests", type=int, default=2000)
     ap.add_argument("--rate", type=float, default=4000.0)
+    ap.add_argument("--rates", default="", help="comma-separated offered rates to sweep (overrides --rate)")
     ap.add_argument("--workers", type=int, default=2)
-    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--reps", type=int, default=3)  # batch: timed repetitions; profile: decompositions
     ap.add_argument("--plain-sample", type=int, default=128)
     ap.add_argument("--seed", type=int, default=1)
     args = ap.parse_args()
     if args.mode == "batch":
         run_batch(args)
-    else:
+    elif args.mode == "serve":
         run_serve(args)
+    elif args.mode == "large":
+        run_large(args)
+    else:
+        run_profile(args)
 
 
 if __name__ == "__main__":

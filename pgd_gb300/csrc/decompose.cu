@@ -21,11 +21,14 @@
 //        c4 = sum_{w in S_q} W(w,p) - |S_q| - sum_{x in T} t(x,q) + 2*k4 + t,
 //     because |N(w) n S_p| = W(w,p) - |N(w) n T| - 1 for w in S_q, and the
 //     edges between S_q and T number sum_{x in T} t(x,q) - 2*k4 - t.
-//     W(w,p) of a hub w is computed once per anchor (a cache), not once per
-//     edge; t(x,q) is read from a per-slot array filled by a triangle pass.
-//   * k4 counts each edge inside T once, from its lower endpoint, by scanning
-//     the degree-oriented list N+(x) (neighbours of higher degree, short even
-//     for hubs) of every x in T.
+//     W(w,p) of every hub w comes from one histogram per anchor (the hub
+//     neighbours of N(p), counted), not from a scan of N(w) per edge; t(x,q)
+//     is read from a per-slot array filled by a triangle pass.
+//   * k4 counts each edge inside T once, from its lower endpoint, as
+//     |N+(x) n T| for every x in T, with N+(x) the degree-oriented list
+//     (neighbours of higher degree).  For the highest-ranked x, N+(x) is also
+//     kept as a bitmap over degree ranks, and |N+(x) n T| is AND + popc of
+//     that row with T's rank bitmap whenever the row is shorter than the list.
 // Anchors of degree >= kAnchorHub are processed by one CTA per (anchor,
 // edge chunk) with N(p) as a bitmap in shared memory (or in a per-CTA global
 // slice when n does not fit); the others by one warp per edge with N(p)
@@ -50,14 +53,18 @@
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kHubWarps = 16;            // hub-anchor CTA: 512 threads
+constexpr int kHubWarps = 32;            // hub-anchor CTA: 1024 threads (latency-bound gathers want warps)
 constexpr int kLightWarps = 8;           // light path: 256 threads, one edge per warp
 constexpr int kAnchorHub = 128;          // default: anchors of degree >= this take the bitmap path
-constexpr int kCacheHub = 64;            // default: W(w,p) cached for neighbours of degree >= this
+constexpr int kCacheHub = 64;            // default: W(w,p) from the histogram for neighbours of degree >= this
 constexpr int kLightStageMax = 256;      // largest warp/block threshold the light path can stage
-constexpr int kChunk = 2048;             // max edges of one anchor per CTA work item
-constexpr uint32_t kPending = 0xffffffffu;
-constexpr int kMaxSmemBitmap = 160 * 1024;
+constexpr int kChunk = 2048;             // edges of one anchor per CTA work item (target)
+constexpr int kMaxChunks = 8;            // ... but an anchor is split into at most this many items, since
+                                         // every item rebuilds the anchor's bitmap and W histogram
+constexpr int kMaxSmemBitmap = 150 * 1024;
+constexpr int kMaxDynSmem = 156 * 1024;  // k_hub dynamic shared memory: bitmap, then the W histogram
+constexpr int kRankBits = 16384;         // T members of degree rank below this are marked in a per-warp bitmap;
+                                         // vertices of rank below this get a rank-bitmap row of N+(x)
 
 inline int grid_for(int64_t n, int per_block = kThreads, int cap = 1 << 20) {
     int64_t g = (n + per_block - 1) / per_block;
@@ -83,8 +90,13 @@ struct DevGraph {
     const int32_t *egraph;      // batched: graph of each E_ordered position, else null
     const long long *gnm;       // batched: n and m of each graph
     const uint8_t *gdense;      // batched: graph decomposed by the row-bitset kernel
-    const int32_t *vrank;       // rank of each vertex by (degree desc, id)
+    const int32_t *vrank;       // rank of each vertex by (degree desc, id desc)
     const int32_t *adjp_rank;   // vrank of each entry of adjp
+    const int64_t *offh;        // hub-neighbour lists (hub ids)
+    const int32_t *adjh;
+    const uint32_t *toprows;    // rank-bitmap rows of N+(x) for vertices of rank < top_r
+    const int4 *vrec;           // per vertex, 32 B: {off, offp} then {deg, |N+|, vrank, hubid}
+    int top_r;
     int anchor_hub;             // anchors of degree >= this take the bitmap path
 };
 
@@ -125,20 +137,72 @@ __global__ void k_oriented_fill(const int64_t *off, const int32_t *adj, const ui
         offp[v] = pos[v < n ? off[v] : nnz];
 }
 
-// degree rank: position in the order (degree descending, id ascending)
+// degree rank: position in the order (degree descending, id descending), so
+// that vrank[a] < vrank[b] exactly when ranks_above(a, b): every entry of
+// N+(x) has a smaller rank than x
 __global__ void k_rank_keys(const int32_t *deg, int64_t n, uint64_t *keys) {
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
-        keys[v] = ((uint64_t)(uint32_t)(0x7fffffff - deg[v]) << 32) | (uint32_t)v;
+        keys[v] = ((uint64_t)(uint32_t)(0x7fffffff - deg[v]) << 32) | (uint32_t)(0x7fffffff - v);
 }
 
 __global__ void k_rank_scatter(const uint64_t *sorted, int64_t n, int32_t *vrank) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        vrank[(uint32_t)(sorted[i] & 0xffffffffu)] = (int32_t)i;
+        vrank[0x7fffffff - (uint32_t)(sorted[i] & 0xffffffffu)] = (int32_t)i;
+}
+
+// Hub-neighbour lists: for every vertex the hub ids of its neighbours that
+// are hubs, in list order.
+__global__ void k_hubnb_flags(const int32_t *adj, const int32_t *hubid, int64_t nnz, uint32_t *flag) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nnz; j += (int64_t)gridDim.x * blockDim.x)
+        flag[j] = hubid[adj[j]] >= 0 ? 1u : 0u;
+}
+
+__global__ void k_hubnb_fill(const int64_t *off, const int32_t *adj, const int32_t *hubid, const uint32_t *flag,
+                             const uint32_t *pos, int64_t n, int64_t nnz, int64_t *offh, int32_t *adjh) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nnz; j += (int64_t)gridDim.x * blockDim.x)
+        if (flag[j]) adjh[pos[j]] = hubid[adj[j]];
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v <= n; v += (int64_t)gridDim.x * blockDim.x)
+        offh[v] = pos[v < n ? off[v] : nnz];
 }
 
 __global__ void k_gather_rank(const int32_t *adjp, const int32_t *vrank, int64_t m, int32_t *out) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
         out[i] = vrank[adjp[i]];
+}
+
+// Rank-bitmap rows: the vertex of rank r < top_r gets a row of (r >> 5) + 1
+// words with bit r_y set for every y in N+(x) (all of rank < r).  Rows are
+// stored back to back in rank order; row r starts at word
+// sum_{r' < r} ((r' >> 5) + 1) = (a + 1) * (16 a + b) for r = 32 a + b.
+__host__ __device__ __forceinline__ int64_t top_row_base(int64_t r) {
+    const int64_t a = r >> 5, b = r & 31;
+    return (a + 1) * (16 * a + b);
+}
+
+__global__ void k_top_rows(const int64_t *offp, const int32_t *adjp_rank, const int32_t *vrank, int64_t n, int top_r,
+                           uint32_t *rows) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t x = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; x < n; x += nw) {
+        const int32_t r = vrank[x];
+        if (r >= top_r) continue;
+        uint32_t *row = rows + top_row_base(r);
+        for (int64_t j = offp[x] + lane; j < offp[x + 1]; j += 32) {
+            const int32_t ry = adjp_rank[j];
+            if (ry < r) atomicOr(row + (ry >> 5), 1u << (ry & 31));
+        }
+    }
+}
+
+// One 32-byte record per vertex with what a scan of N(q) needs to know about
+// each neighbour w, so that one sector load replaces six dependent ones.
+__global__ void k_vrec(const int64_t *off, const int64_t *offp, const int32_t *deg, const int32_t *vrank,
+                       const int32_t *hubid, int64_t n, int4 *vrec) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t o = off[v], op = offp[v];
+        vrec[2 * v] = make_int4((int)(uint32_t)o, (int)(o >> 32), (int)(uint32_t)op, (int)(op >> 32));
+        vrec[2 * v + 1] = make_int4(deg[v], (int)(offp[v + 1] - op), vrank[v], hubid[v]);
+    }
 }
 
 __global__ void k_hub_flags(const int32_t *deg, int64_t n, int cache_hub, uint32_t *flag) {
@@ -176,10 +240,11 @@ __global__ void k_tslot(DevGraph G, uint32_t *tslot) {
 // ---------------------------------------------------------------------------
 // work plan: hub-anchored edges grouped by anchor, light edges listed
 
-// key = (anchor << 32 | position) for hub-anchored edges, (~0 << 32 | position)
-// for the rest, so one sort groups the first and lists the second in order.
-// Dense-graph edges (batches only) get 0xfffffffe, so the sorted order is
-// [hub-anchored, by anchor][dense][light].
+// key = (rank(anchor) << 32 | position) for hub-anchored edges,
+// (~0 << 32 | position) for the rest, so one sort groups the first, highest
+// degree anchors first (the largest work items are handed out first), and
+// lists the second in order.  Dense-graph edges (batches only) get
+// 0xfffffffe, so the sorted order is [hub-anchored, by anchor][dense][light].
 __global__ void k_plan_keys(DevGraph G, uint64_t *keys, unsigned long long *counts) {
     unsigned long long hubs = 0, dense = 0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < G.m; e += (int64_t)gridDim.x * blockDim.x) {
@@ -188,7 +253,7 @@ __global__ void k_plan_keys(DevGraph G, uint64_t *keys, unsigned long long *coun
         const int32_t p = ranks_above(v, u, G.deg) ? v : u;
         const bool d = dense_edge(G, e);
         const bool hub = !d && G.deg[p] >= G.anchor_hub;
-        const uint32_t hi = d ? 0xfffffffeu : (hub ? (uint32_t)p : 0xffffffffu);
+        const uint32_t hi = d ? 0xfffffffeu : (hub ? (uint32_t)G.vrank[p] : 0xffffffffu);
         keys[e] = ((uint64_t)hi << 32) | (uint32_t)e;
         hubs += hub;
         dense += d;
@@ -201,7 +266,8 @@ __global__ void k_plan_keys(DevGraph G, uint64_t *keys, unsigned long long *coun
     }
 }
 
-// item i starts a chunk: first edge of an anchor, or every kChunk-th of it
+// item i starts a chunk: the first edge of an anchor's run of L edges, or
+// every c-th of it, c = ceil(L / min(ceil(L / kChunk), kMaxChunks))
 __global__ void k_item_flags(const uint64_t *keys, int64_t nh, uint32_t *flag) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nh; i += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t p = (uint32_t)(keys[i] >> 32);
@@ -211,7 +277,16 @@ __global__ void k_item_flags(const uint64_t *keys, int64_t nh, uint32_t *flag) {
             int64_t mid = (lo + hi) >> 1;
             if ((uint32_t)(keys[mid] >> 32) < p) lo = mid + 1; else hi = mid;
         }
-        flag[i] = ((i - lo) % kChunk == 0) ? 1u : 0u;
+        // one past its last index
+        int64_t lo2 = i + 1, hi2 = nh;
+        while (lo2 < hi2) {
+            int64_t mid = (lo2 + hi2) >> 1;
+            if ((uint32_t)(keys[mid] >> 32) <= p) lo2 = mid + 1; else hi2 = mid;
+        }
+        const int64_t L = lo2 - lo;
+        const int64_t chunks = min((L + kChunk - 1) / kChunk, (int64_t)kMaxChunks);
+        const int64_t c = (L + chunks - 1) / chunks;
+        flag[i] = ((i - lo) % c == 0) ? 1u : 0u;
     }
 }
 
@@ -299,26 +374,31 @@ __device__ __forceinline__ bool bit_of(const uint32_t *bm, int32_t x) { return (
 // ---------------------------------------------------------------------------
 // Hub anchors: one CTA per (anchor, chunk of its edges).
 //
-// Per work item: (1) N(p) into the bitmap; (2) every hub w adjacent to a q
-// of the chunk but not to p is claimed in this CTA's W cache and queued;
-// (3) the queue is drained, one warp per W(w,p); (4) the chunk's edges are
-// decomposed, one warp each, fetched dynamically.  Per edge the warp first
-// collects T (sorted, in shared memory when it fits), t and the cached W's,
-// then scans the remaining lists: N(w) of non-hub w in S_q (W by bit tests)
-// and N+(x) of x in T (k4 by bit test and T membership).  Lists of 32 or more
-// entries are read warp-cooperatively with four loads in flight per lane;
-// shorter ones are flattened across the warp.
-
-constexpr int kRankBits = 16384;         // T members of degree rank below this are marked in a per-warp bitmap
-constexpr int kQueue = 2048;             // queued W computations per CTA
+// Per work item: (1) N(p) goes into the bitmap and, in the same pass, the
+// hub-neighbour lists of N(p) are histogrammed: afterwards hist[h] =
+// |N(w_h) n N(p)| = W(w_h, p) for every hub w_h, whatever q needs it.
+// (2) The chunk's edges are decomposed, one warp each, fetched dynamically.
+// Per edge the warp first collects T (marked by degree rank in a per-warp
+// bitmap), t, sum t(x,q) and the W's of hub neighbours, then scans what is
+// left: N(w) of non-hub w in S_q (W by bit tests in the N(p) bitmap) and, for
+// k4, |N+(x) n T| of x in T, either from x's oriented list or, for the
+// highest-ranked x, as AND + popc of x's rank-bitmap row with the T bitmap.
+// Lists of 64 or more entries are read warp-cooperatively; shorter ones are
+// flattened across the warp, two loads in flight per lane.  Each neighbour w
+// of q is described by one 32-byte record (offsets, |N+(w)|, rank, hub id);
+// for q of degree <= 32, the first pass keeps what the second scans in
+// registers.
 
 struct HubArgs {
     DevGraph G;
     const int32_t *hpos;      // E_ordered positions of hub-anchored edges, grouped by anchor
     const int64_t *items;     // chunk starts into hpos, nitems+1 entries
     int64_t nitems;
-    unsigned long long *cache;  // per CTA: nhubs entries (anchor << 32 | W)
+    uint32_t *ghist;          // per CTA histogram slices (hstride words each) when not in shared memory
     int32_t nhubs;
+    int64_t hstride;
+    int smem_hist;
+    int hist16;               // two 16-bit counters per word (every W < 65536: max degree below that)
     uint32_t *gbitmap;        // per CTA bitmap slices when not in shared memory
     int64_t nwords;
     int smem_bitmap;
@@ -337,6 +417,15 @@ __device__ __forceinline__ unsigned count_bits(const uint32_t *bm, const int32_t
     return c;
 }
 
+// sum over words of popc(row & Rw), warp-cooperative
+__device__ __forceinline__ unsigned row_and_count(const uint32_t *row, const uint32_t *Rw, int words, int lane) {
+    unsigned c = 0;
+    int i = lane;
+    for (; i + 32 < words; i += 64) c += __popc(__ldg(row + i) & Rw[i]) + __popc(__ldg(row + i + 32) & Rw[i + 32]);
+    if (i < words) c += __popc(__ldg(row + i) & Rw[i]);
+    return c;
+}
+
 // y in T = N(p) n N(q).  Almost every y tested is a high-degree vertex, so
 // T's members of degree rank < kRankBits are marked in a per-warp bitmap and
 // the test is one shared-memory bit; other y fall back to the p bitmap and a
@@ -347,35 +436,111 @@ __device__ __forceinline__ bool in_t(const uint32_t *Rw, const uint32_t *bm, con
     return bit_of(bm, y) && pgd_contains(Nq, dq, y);
 }
 
+// Histogram of the hub ids in the lists of the 32 vertices the warp holds
+// (one per lane, len entries at list): long lists warp-cooperatively, the
+// rest flattened.  H is a shared or a global pointer (distinct code paths so
+// that shared-memory atomics stay shared).
+// Returns the number of entries visited (the same in every lane).
+template <typename AddFn>
+__device__ __forceinline__ int hist_lists(const int32_t *list, int len, int lane, AddFn add) {
+    int visited = __reduce_add_sync(0xffffffffu, (unsigned)len);
+    unsigned longm = __ballot_sync(0xffffffffu, len >= 64);
+    while (longm) {
+        const int src = __ffs(longm) - 1;
+        longm &= longm - 1;
+        const int32_t *L = (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)list, src);
+        const int ln = __shfl_sync(0xffffffffu, len, src);
+        int i = lane;
+        for (; i + 32 < ln; i += 64) {
+            const int32_t h0 = __ldg(L + i), h1 = __ldg(L + i + 32);
+            add(h0);
+            add(h1);
+        }
+        if (i < ln) add(__ldg(L + i));
+    }
+    if (len >= 64) len = 0;
+    const int incl = pgd_warp_incl_scan(len);
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int excl = incl - len;
+    for (int b2 = 0; b2 < total; b2 += 32) {
+        const int it = b2 + lane;
+        const int own = owner_of(incl, it);
+        const int32_t *olist = (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)list, own);
+        const int oexcl = __shfl_sync(0xffffffffu, excl, own);
+        if (it < total) add(__ldg(olist + (it - oexcl)));
+    }
+    return visited;
+}
+
+__device__ __forceinline__ int64_t rec_off(const int4 &ra) { return (int64_t)(((uint64_t)(uint32_t)ra.y << 32) | (uint32_t)ra.x); }
+__device__ __forceinline__ int64_t rec_offp(const int4 &ra) { return (int64_t)(((uint64_t)(uint32_t)ra.w << 32) | (uint32_t)ra.z); }
+
+// What pass 2 scans for neighbour w of q (records ra, rb): for w in T, N+(w)
+// as a list (kind 1) or a rank-bitmap row (kind 2); for a non-hub w outside
+// N(p), N(w) (kind 0); nothing otherwise (len 0).
+__device__ __forceinline__ void plan_entry(const DevGraph &G, bool inT, const int4 &ra, const int4 &rb, int &len,
+                                           int &kind, const int32_t *&list, const int32_t *&rlist) {
+    if (inT) {
+        const int32_t r = rb.z;
+        const int dplus = rb.y, words = (r >> 5) + 1;
+        if (r < G.top_r && words < dplus) {
+            kind = 2;
+            len = words;
+            list = (const int32_t *)(G.toprows + top_row_base(r));
+        } else {
+            const int64_t o = rec_offp(ra);
+            kind = 1;
+            len = dplus;
+            list = G.adjp + o;
+            rlist = G.adjp_rank + o;
+        }
+    } else if (rb.w < 0) {
+        kind = 0;
+        len = rb.x;
+        list = G.adj + rec_off(ra);
+    }
+}
+
 __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
-    extern __shared__ uint32_t s_bits[];
+    extern __shared__ __align__(16) uint32_t s_dyn[];
     __shared__ unsigned long long s_red[kHubWarps][PGD_NSUMS];
     __shared__ uint32_t s_R[kHubWarps][kRankBits / 32];
-    __shared__ int32_t s_qw[kQueue];
-    __shared__ int32_t s_qh[kQueue];
     __shared__ long long s_item;
-    __shared__ int s_qlen, s_qnext, s_enext_a, s_enext_c;
+    __shared__ int s_enext;
+    __shared__ unsigned long long s_hcount;
     const DevGraph &G = A.G;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     uint32_t *Rw = s_R[wid];
     for (int i = lane; i < kRankBits / 32; i += 32) Rw[i] = 0;
-    uint32_t *bm = A.smem_bitmap ? s_bits : A.gbitmap + (int64_t)blockIdx.x * A.nwords;
-    unsigned long long *cache = A.cache + (int64_t)blockIdx.x * A.nhubs;
+    uint32_t *bm = A.smem_bitmap ? s_dyn : A.gbitmap + (int64_t)blockIdx.x * A.nwords;
+    // histogram: shared (after the bitmap, 16-byte aligned) or this CTA's global slice
+    uint32_t *sh_hist = s_dyn + (A.smem_bitmap ? ((A.nwords + 3) & ~(int64_t)3) : 0);
+    uint32_t *gl_hist = A.ghist + (int64_t)blockIdx.x * A.hstride;
+    const bool smem_hist = A.smem_hist != 0;
+    const bool h16 = A.hist16 != 0;
+    // this warp's partial sums live in shared memory (lane 0 updates them),
+    // which keeps 30 registers free for the gathers
+    unsigned long long *acc = s_red[wid];
+    if (lane < PGD_NSUMS) acc[lane] = 0;
+    const int nh4 = (int)(A.hstride >> 2);
+    // counter h: word and increment (16-bit halves never carry: W < 65536)
+    auto hw = [h16](int32_t h) { return h16 ? (h >> 1) : h; };
+    auto hinc = [h16](int32_t h) { return h16 ? (1u << ((h & 1) << 4)) : 1u; };
+    auto hval = [h16](uint32_t word, int32_t h) { return h16 ? ((word >> ((h & 1) << 4)) & 0xffffu) : word; };
     int cur_g = -1;
-    unsigned long long acc[PGD_NSUMS];
-#pragma unroll
-    for (int i = 0; i < PGD_NSUMS; i++) acc[i] = 0;
     if (A.smem_bitmap)
         for (int64_t i = threadIdx.x; i < A.nwords; i += blockDim.x) bm[i] = 0;
+    {
+        uint4 *h4 = (uint4 *)(smem_hist ? sh_hist : gl_hist);
+        for (int i = threadIdx.x; i < nh4; i += blockDim.x) h4[i] = make_uint4(0, 0, 0, 0);
+    }
     __syncthreads();
 
     while (true) {
         if (threadIdx.x == 0) {
             s_item = (long long)atomicAdd(A.next, 1ull);
-            s_qlen = 0;
-            s_qnext = 0;
-            s_enext_a = 0;
-            s_enext_c = 0;
+            s_enext = 0;
+            s_hcount = 0;
         }
         __syncthreads();
         const long long item = s_item;
@@ -390,80 +555,34 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
         }
         const int dp = G.deg[p];
         const int32_t *Np = G.adj + G.off[p];
-        for (int i = threadIdx.x; i < dp; i += blockDim.x) {
-            const int32_t y = __ldg(Np + i);
-            atomicOr(bm + (y >> 5), 1u << (y & 31));
-        }
-        __syncthreads();
 
-        // ---- (2) claim the hub neighbours whose W(w,p) is needed ----------
-        while (true) {
-            int k = 0;
-            if (lane == 0) k = atomicAdd(&s_enext_a, 1);
-            k = __shfl_sync(0xffffffffu, k, 0);
-            if (k >= nedge) break;
-            const int32_t id = G.order[A.hpos[start + k]];
-            const int32_t q = (G.ev[id] == p) ? G.eu[id] : G.ev[id];
-            const int dq = G.deg[q];
-            const int32_t *Nq = G.adj + G.off[q];
-            for (int base = 0; base < dq; base += 32) {
-                const int j = base + lane;
-                bool claim = false;
-                int32_t w = -1, h = -1;
-                if (j < dq) {
-                    w = __ldg(Nq + j);
-                    if (w != p && !bit_of(bm, w) && (h = G.hubid[w]) >= 0) {
-                        const unsigned long long ent = cache[h];
-                        if ((uint32_t)(ent >> 32) != (uint32_t)p) {
-                            const unsigned long long mine = ((unsigned long long)(uint32_t)p << 32) | kPending;
-                            claim = atomicCAS(cache + h, ent, mine) == ent;
-                        }
-                    }
-                }
-                const unsigned mask = __ballot_sync(0xffffffffu, claim);
-                if (!mask) continue;
-                int slot = 0;
-                if (lane == 0) slot = atomicAdd(&s_qlen, __popc(mask));
-                slot = __shfl_sync(0xffffffffu, slot, 0) + __popc(mask & ((1u << lane) - 1));
-                if (claim && slot < kQueue) {
-                    s_qw[slot] = w;
-                    s_qh[slot] = h;
-                }
-                // queue full: compute here
-                unsigned over = __ballot_sync(0xffffffffu, claim && slot >= kQueue);
-                while (over) {
-                    const int src = __ffs(over) - 1;
-                    over &= over - 1;
-                    const int32_t wc = __shfl_sync(0xffffffffu, w, src);
-                    const int32_t hc = __shfl_sync(0xffffffffu, h, src);
-                    unsigned long long c = count_bits(bm, G.adj + G.off[wc], G.deg[wc], lane);
-                    c = pgd_warp_sum(c);
-                    if (lane == 0) cache[hc] = ((unsigned long long)(uint32_t)p << 32) | (uint32_t)c;
-                }
-            }
-        }
-        __syncthreads();
-
-        // ---- (3) drain the queue ------------------------------------------
+        // ---- (1) N(p) bitmap and the W histogram --------------------------
         {
-            const int qlen = min(s_qlen, kQueue);
-            while (true) {
-                int k = 0;
-                if (lane == 0) k = atomicAdd(&s_qnext, 1);
-                k = __shfl_sync(0xffffffffu, k, 0);
-                if (k >= qlen) break;
-                const int32_t w = s_qw[k];
-                unsigned long long c = count_bits(bm, G.adj + G.off[w], G.deg[w], lane);
-                c = pgd_warp_sum(c);
-                if (lane == 0) cache[s_qh[k]] = ((unsigned long long)(uint32_t)p << 32) | (uint32_t)c;
+            unsigned long long visited = 0;
+            for (int base = wid * 32; base < dp; base += kHubWarps * 32) {
+                const int j = base + lane;
+                int len = 0;
+                const int32_t *list = nullptr;
+                if (j < dp) {
+                    const int32_t x = __ldg(Np + j);
+                    atomicOr(bm + (x >> 5), 1u << (x & 31));
+                    const int64_t o = G.offh[x];
+                    len = (int)(G.offh[x + 1] - o);
+                    list = G.adjh + o;
+                }
+                if (smem_hist)
+                    visited += hist_lists(list, len, lane, [&](int32_t h) { atomicAdd(sh_hist + hw(h), hinc(h)); });
+                else
+                    visited += hist_lists(list, len, lane, [&](int32_t h) { atomicAdd(gl_hist + hw(h), hinc(h)); });
             }
+            if (lane == 0 && visited) atomicAdd(&s_hcount, visited);
         }
         __syncthreads();
 
-        // ---- (4) the chunk's edges ---------------------------------------
+        // ---- (2) the chunk's edges ---------------------------------------
         while (true) {
             int k = 0;
-            if (lane == 0) k = atomicAdd(&s_enext_c, 1);
+            if (lane == 0) k = atomicAdd(&s_enext, 1);
             k = __shfl_sync(0xffffffffu, k, 0);
             if (k >= nedge) break;
             const int64_t e = A.hpos[start + k];
@@ -473,60 +592,67 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
             const int dq = G.deg[q];
             const int64_t offq = G.off[q];
             const int32_t *Nq = G.adj + offq;
-            // pass 1: T (sorted), t, sum of t(x,q) over T, cached W's
+            // pass 1: T (rank bitmap), t, sum of t(x,q) over T, W's of hubs;
+            // for q of degree <= 32 also what pass 2 scans, kept in registers
             unsigned t = 0;
             unsigned long long sumtq = 0, sumW = 0, k4 = 0;
+            int len0 = 0, kind0 = 0;
+            const int32_t *list0 = nullptr, *rlist0 = nullptr;
             for (int base = 0; base < dq; base += 32) {
                 const int j = base + lane;
                 bool inT = false;
                 if (j < dq) {
                     const int32_t w = __ldg(Nq + j);
                     if (w != p) {
-                        if (bit_of(bm, w)) {
-                            inT = true;
-                            sumtq += G.tslot[offq + j];
-                            const int32_t r = G.vrank[w];
+                        const int4 ra = __ldg(G.vrec + 2 * (int64_t)w), rb = __ldg(G.vrec + 2 * (int64_t)w + 1);
+                        const uint32_t tq = __ldg(G.tslot + offq + j);
+                        inT = bit_of(bm, w);
+                        if (inT) {
+                            sumtq += tq;
+                            const int32_t r = rb.z;
                             if (r < kRankBits) atomicOr(Rw + (r >> 5), 1u << (r & 31));
                         } else {
-                            const int32_t h = G.hubid[w];
-                            if (h >= 0) sumW += (uint32_t)cache[h];
+                            const int32_t h = rb.w;
+                            if (h >= 0) sumW += hval(smem_hist ? sh_hist[hw(h)] : __ldcg(gl_hist + hw(h)), h);
                         }
+                        if (dq <= 32) plan_entry(G, inT, ra, rb, len0, kind0, list0, rlist0);
                     }
                 }
                 t += __popc(__ballot_sync(0xffffffffu, inT));
             }
             __syncwarp();
-            // pass 2: scan N(w) of non-hub w in S_q and N+(x) of x in T
+            // pass 2: N(w) of non-hub w in S_q (kind 0), N+(x) of x in T as a
+            // list (kind 1) or as a rank-bitmap row (kind 2)
             for (int base = 0; base < dq; base += 32) {
-                const int j = base + lane;
-                int len = 0, kind = 0;
-                const int32_t *list = nullptr;
-                const int32_t *rlist = nullptr;
-                if (j < dq) {
-                    const int32_t w = __ldg(Nq + j);
-                    if (w != p) {
-                        if (bit_of(bm, w)) {
-                            kind = 1;
-                            const int64_t o = G.offp[w];
-                            len = (int)(G.offp[w + 1] - o);
-                            list = G.adjp + o;
-                            rlist = G.adjp_rank + o;
-                        } else if (G.hubid[w] < 0) {
-                            len = G.deg[w];
-                            list = G.adj + G.off[w];
+                int len = len0, kind = kind0;
+                const int32_t *list = list0;
+                const int32_t *rlist = rlist0;
+                if (dq > 32) {
+                    const int j = base + lane;
+                    len = 0;
+                    kind = 0;
+                    list = rlist = nullptr;
+                    if (j < dq) {
+                        const int32_t w = __ldg(Nq + j);
+                        if (w != p) {
+                            const int4 ra = __ldg(G.vrec + 2 * (int64_t)w), rb = __ldg(G.vrec + 2 * (int64_t)w + 1);
+                            plan_entry(G, bit_of(bm, w), ra, rb, len, kind, list, rlist);
                         }
                     }
                 }
-                // long lists: one at a time, warp-cooperative
-                unsigned longm = __ballot_sync(0xffffffffu, len >= 32);
+                // long lists (>= 64 entries): one at a time, warp-cooperative
+                unsigned longm = __ballot_sync(0xffffffffu, len >= 64);
                 while (longm) {
                     const int src = __ffs(longm) - 1;
                     longm &= longm - 1;
                     const int32_t *L = (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)list, src);
                     const int32_t *LR = (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)rlist, src);
                     const int ln = __shfl_sync(0xffffffffu, len, src);
-                    if (__shfl_sync(0xffffffffu, kind, src) == 0) {
+                    const int lk = __shfl_sync(0xffffffffu, kind, src);
+                    if (lk == 0) {
                         sumW += count_bits(bm, L, ln, lane);
+                    } else if (lk == 2) {
+                        k4 += row_and_count((const uint32_t *)L, Rw, ln, lane);
                     } else {
                         int i = lane;
                         for (; i + 32 < ln; i += 64) {
@@ -538,23 +664,34 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                     }
                 }
                 // short lists: flattened over the warp
-                if (len >= 32) len = 0;
+                if (len >= 64) len = 0;
                 const int incl = pgd_warp_incl_scan(len);
                 const int total = __shfl_sync(0xffffffffu, incl, 31);
                 const int excl = incl - len;
-                for (int b2 = 0; b2 < total; b2 += 32) {
-                    const int it = b2 + lane;
-                    const int own = owner_of(incl, it);
-                    const int32_t *olist =
-                        (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)list, own);
-                    const int32_t *orank =
-                        (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)rlist, own);
-                    const int okind = __shfl_sync(0xffffffffu, kind, own);
-                    const int oexcl = __shfl_sync(0xffffffffu, excl, own);
-                    if (it < total) {
-                        const int32_t x = __ldg(olist + (it - oexcl));
-                        if (okind == 0) sumW += bit_of(bm, x);
-                        else k4 += in_t(Rw, bm, Nq, dq, x, __ldg(orank + (it - oexcl))) ? 1 : 0;
+                for (int b2 = 0; b2 < total; b2 += 64) {
+                    const int itA = b2 + lane, itB = b2 + 32 + lane;
+                    const int ownA = owner_of(incl, itA), ownB = owner_of(incl, itB);
+                    const int32_t *olA = (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)list, ownA);
+                    const int32_t *orA = (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)rlist, ownA);
+                    const int okA = __shfl_sync(0xffffffffu, kind, ownA);
+                    const int idxA = itA - __shfl_sync(0xffffffffu, excl, ownA);
+                    const int32_t *olB = (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)list, ownB);
+                    const int32_t *orB = (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)rlist, ownB);
+                    const int okB = __shfl_sync(0xffffffffu, kind, ownB);
+                    const int idxB = itB - __shfl_sync(0xffffffffu, excl, ownB);
+                    const bool vA = itA < total, vB = itB < total;
+                    const int32_t xA = vA ? __ldg(olA + idxA) : 0, xB = vB ? __ldg(olB + idxB) : 0;
+                    const int32_t rA = (vA && okA == 1) ? __ldg(orA + idxA) : 0;
+                    const int32_t rB = (vB && okB == 1) ? __ldg(orB + idxB) : 0;
+                    if (vA) {
+                        if (okA == 0) sumW += bit_of(bm, xA);
+                        else if (okA == 2) k4 += __popc((uint32_t)xA & Rw[idxA]);
+                        else k4 += in_t(Rw, bm, Nq, dq, xA, rA) ? 1 : 0;
+                    }
+                    if (vB) {
+                        if (okB == 0) sumW += bit_of(bm, xB);
+                        else if (okB == 2) k4 += __popc((uint32_t)xB & Rw[idxB]);
+                        else k4 += in_t(Rw, bm, Nq, dq, xB, rB) ? 1 : 0;
                     }
                 }
             }
@@ -570,6 +707,26 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
         }
         __syncthreads();
         for (int i = threadIdx.x; i < dp; i += blockDim.x) bm[__ldg(Np + i) >> 5] = 0;
+        if (s_hcount * 4 >= (unsigned long long)A.nhubs) {
+            uint4 *h4 = (uint4 *)(smem_hist ? sh_hist : gl_hist);
+            for (int i = threadIdx.x; i < nh4; i += blockDim.x) h4[i] = make_uint4(0, 0, 0, 0);
+        } else {
+            // few entries touched (large graphs, small anchors): clear just those
+            for (int base = wid * 32; base < dp; base += kHubWarps * 32) {
+                const int j = base + lane;
+                int len = 0;
+                const int32_t *list = nullptr;
+                if (j < dp) {
+                    const int32_t x = __ldg(Np + j);
+                    const int64_t o = G.offh[x];
+                    len = (int)(G.offh[x + 1] - o);
+                    list = G.adjh + o;
+                }
+                // (a shared 16-bit word's other counter is zero or cleared too)
+                if (smem_hist) hist_lists(list, len, lane, [&](int32_t h) { sh_hist[hw(h)] = 0; });
+                else hist_lists(list, len, lane, [&](int32_t h) { gl_hist[hw(h)] = 0; });
+            }
+        }
         __syncthreads();
     }
     block_flush(G, acc, cur_g, s_red, kHubWarps);
@@ -810,6 +967,11 @@ static pgd_status build_aux(pgd_graph *g) {
         if ((st = pgd_graph_alloc(g, (void **)&g->adjp_rank, (g->m + 1) * sizeof(int32_t)))) return st;
         if ((st = pgd_graph_alloc(g, (void **)&g->hubid, (n + 1) * sizeof(int32_t)))) return st;
         if ((st = pgd_graph_alloc(g, (void **)&g->tslot, (nnz + 1) * sizeof(uint32_t)))) return st;
+        if ((st = pgd_graph_alloc(g, (void **)&g->offh, (n + 1) * sizeof(int64_t)))) return st;
+        if ((st = pgd_graph_alloc(g, (void **)&g->vrec, (n + 1) * 32))) return st;
+        g->top_r = (int32_t)std::min<int64_t>(n, kRankBits);
+        g->top_words = top_row_base(g->top_r);
+        if ((st = pgd_graph_alloc(g, (void **)&g->toprows, (g->top_words + 1) * sizeof(uint32_t)))) return st;
     }
     int32_t *row = nullptr;
     uint32_t *flag = nullptr, *pos = nullptr;
@@ -838,6 +1000,27 @@ static pgd_status build_aux(pgd_graph *g) {
     cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, n + 1, s);
     pgd_tmp_free(ctx, tmp);
     PGD_LAUNCH(ctx, k_hub_ids, grid_for(n), kThreads, 0, flag, pos, n, g->hubid);
+    uint32_t nh = 0;
+    PGD_CUDA(ctx, cudaMemcpyAsync(&nh, pos + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    // hub-neighbour lists (their length depends on the hub threshold)
+    PGD_LAUNCH(ctx, k_hubnb_flags, grid_for(nnz), kThreads, 0, g->adj, g->hubid, nnz, flag);
+    PGD_CUDA(ctx, cudaMemsetAsync(flag + nnz, 0, sizeof(uint32_t), s));
+    tb = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tb, flag, pos, nnz + 1, s);
+    if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
+    cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, nnz + 1, s);
+    pgd_tmp_free(ctx, tmp);
+    {
+        uint32_t nadjh = 0;
+        PGD_CUDA(ctx, cudaMemcpyAsync(&nadjh, pos + nnz, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        PGD_CUDA(ctx, cudaStreamSynchronize(s));
+        pgd_graph_free(g, g->adjh, (g->nadjh + 1) * sizeof(int32_t));
+        g->adjh = nullptr;
+        g->nadjh = nadjh;
+        if ((st = pgd_graph_alloc(g, (void **)&g->adjh, (g->nadjh + 1) * sizeof(int32_t)))) return st;
+    }
+    PGD_LAUNCH(ctx, k_hubnb_fill, grid_for(std::max(nnz, n + 1)), kThreads, 0, g->off, g->adj, g->hubid, flag, pos, n,
+               nnz, g->offh, g->adjh);
     // degree ranks of the vertices and of the oriented list entries
     {
         uint64_t *rk = nullptr, *rk2 = nullptr;
@@ -856,8 +1039,15 @@ static pgd_status build_aux(pgd_graph *g) {
         pgd_tmp_free(ctx, rk);
         pgd_tmp_free(ctx, rk2);
     }
-    uint32_t nh = 0;
-    PGD_CUDA(ctx, cudaMemcpyAsync(&nh, pos + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    if (n > 0)
+        PGD_LAUNCH(ctx, k_vrec, grid_for(n), kThreads, 0, g->off, g->offp, g->deg, g->vrank, g->hubid, n,
+                   (int4 *)g->vrec);
+    // rank-bitmap rows of the highest-ranked vertices (ranks do not depend on
+    // the thresholds, so a rebuild for new thresholds recomputes the same rows)
+    PGD_CUDA(ctx, cudaMemsetAsync(g->toprows, 0, (g->top_words + 1) * sizeof(uint32_t), s));
+    if (g->top_r > 0 && g->m > 0)
+        PGD_LAUNCH(ctx, k_top_rows, grid_for(32 * n), kThreads, 0, g->offp, g->adjp_rank, g->vrank, n, g->top_r,
+                   g->toprows);
     PGD_CUDA(ctx, cudaStreamSynchronize(s));
     g->nhubs = (int32_t)nh;
     pgd_tmp_free(ctx, row);
@@ -890,6 +1080,11 @@ static DevGraph dev_view(pgd_graph *g, bool micro) {
     G.gdense = nullptr;
     G.vrank = g->vrank;
     G.adjp_rank = g->adjp_rank;
+    G.offh = g->offh;
+    G.adjh = g->adjh;
+    G.toprows = g->toprows;
+    G.vrec = (const int4 *)g->vrec;
+    G.top_r = g->top_r;
     G.anchor_hub = g->ctx->anchor_hub;
     return G;
 }
@@ -902,8 +1097,23 @@ struct DenseView {
     const int64_t *vbase;
 };
 
-static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, uint32_t *tslot, int32_t nhubs, float *ms,
-                                const DenseView *dense = nullptr) {
+// Where k_hub keeps the N(p) bitmap and the W histogram: shared memory when
+// they fit (the bitmap first), else per-CTA global slices.  Fills the layout
+// fields of H and returns the dynamic shared memory size.
+static size_t hub_layout(int64_t n, int32_t nhubs, int32_t max_degree, HubArgs *H) {
+    H->nwords = (n + 31) / 32;
+    H->nhubs = nhubs;
+    H->hist16 = max_degree < 65536 ? 1 : 0;
+    const int64_t hwords = H->hist16 ? ((int64_t)nhubs + 1) / 2 : (int64_t)nhubs;
+    H->hstride = std::max<int64_t>(4, (hwords + 3) & ~(int64_t)3);
+    H->smem_bitmap = H->nwords * 4 <= kMaxSmemBitmap ? 1 : 0;
+    const int64_t bm_bytes = H->smem_bitmap ? ((H->nwords + 3) & ~(int64_t)3) * 4 : 0;
+    H->smem_hist = bm_bytes + H->hstride * 4 <= kMaxDynSmem ? 1 : 0;
+    return (size_t)(bm_bytes + (H->smem_hist ? H->hstride * 4 : 0));
+}
+
+static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, uint32_t *tslot, int32_t nhubs, int32_t max_degree,
+                                float *ms, const DenseView *dense = nullptr) {
     cudaStream_t s = ctx->stream;
     pgd_status st;
     const int64_t m = G.m;
@@ -913,7 +1123,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, uint32_t *tslot
     int32_t *posv = nullptr;
     uint32_t *flag = nullptr, *fpos = nullptr;
     int64_t *items = nullptr;
-    unsigned long long *cache = nullptr;
+    uint32_t *ghist = nullptr;
     uint32_t *gbm = nullptr;
     if ((st = pgd_tmp_alloc(ctx, (void **)&keys, m * sizeof(uint64_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&keys2, m * sizeof(uint64_t)))) return st;
@@ -956,27 +1166,22 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, uint32_t *tslot
     }
     const int nsm = ctx->num_sms;
     if (nitems > 0) {
-        const int64_t nwords = (G.n + 31) / 32;
-        const bool in_smem = nwords * 4 <= kMaxSmemBitmap;
-        size_t smem = in_smem ? (size_t)nwords * 4 : 0;
-        const int nh_slots = std::max(1, (int)nhubs);
-        if ((st = pgd_tmp_alloc(ctx, (void **)&cache, (size_t)nsm * nh_slots * sizeof(unsigned long long)))) return st;
-        PGD_CUDA(ctx, cudaMemsetAsync(cache, 0xff, (size_t)nsm * nh_slots * sizeof(unsigned long long), s));
-        if (!in_smem) {
-            if ((st = pgd_tmp_alloc(ctx, (void **)&gbm, (size_t)nsm * nwords * 4))) return st;
-            PGD_CUDA(ctx, cudaMemsetAsync(gbm, 0, (size_t)nsm * nwords * 4, s));
+        HubArgs H;
+        const size_t smem = hub_layout(G.n, nhubs, max_degree, &H);
+        if (!H.smem_bitmap) {
+            if ((st = pgd_tmp_alloc(ctx, (void **)&gbm, (size_t)nsm * H.nwords * 4))) return st;
+            PGD_CUDA(ctx, cudaMemsetAsync(gbm, 0, (size_t)nsm * H.nwords * 4, s));
+        }
+        if (!H.smem_hist) {
+            if ((st = pgd_tmp_alloc(ctx, (void **)&ghist, (size_t)nsm * H.hstride * 4))) return st;
         }
         PGD_CUDA(ctx, cudaFuncSetAttribute(k_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        HubArgs H;
         H.G = G;
         H.hpos = posv;
         H.items = items;
         H.nitems = nitems;
-        H.cache = cache;
-        H.nhubs = nh_slots;
+        H.ghist = ghist;
         H.gbitmap = gbm;
-        H.nwords = nwords;
-        H.smem_bitmap = in_smem ? 1 : 0;
         H.next = ctr + 1;
         PGD_LAUNCH(ctx, k_hub, nsm, kHubWarps * 32, smem, H);
     }
@@ -1007,7 +1212,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, uint32_t *tslot
     pgd_tmp_free(ctx, flag);
     pgd_tmp_free(ctx, fpos);
     pgd_tmp_free(ctx, items);
-    pgd_tmp_free(ctx, cache);
+    pgd_tmp_free(ctx, ghist);
     pgd_tmp_free(ctx, gbm);
     PGD_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
     PGD_CUDA(ctx, cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
@@ -1024,7 +1229,7 @@ pgd_status pgd_dev_decompose(pgd_graph *g, bool micro, pgd_counts *out) {
     if ((!g->has_aux || g->aux_cache_hub != ctx->cache_hub) && (st = build_aux(g))) return st;
     PGD_CUDA(ctx, cudaMemsetAsync(ctx->d_sums, 0, PGD_NSUMS * sizeof(unsigned long long), s));
     float ms = 0;
-    if ((st = run_decompose(ctx, dev_view(g, micro), g->tslot, g->nhubs, &ms))) return st;
+    if ((st = run_decompose(ctx, dev_view(g, micro), g->tslot, g->nhubs, g->max_degree, &ms))) return st;
     unsigned long long h[PGD_NSUMS];
     PGD_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_sums, sizeof(h), cudaMemcpyDeviceToHost, s));
     PGD_CUDA(ctx, cudaStreamSynchronize(s));
@@ -1099,6 +1304,7 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
     std::vector<int64_t> bases((size_t)3 * k + 3, 0);
     std::vector<long long> gnm((size_t)2 * k);
     int64_t N = 0, M = 0, S = 0;
+    int32_t max_degree = 0;
     for (int i = 0; i < k; i++) {
         pgd_graph *g = graphs[i];
         if (micro && !g->micro) {
@@ -1121,6 +1327,7 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
         bases[(size_t)2 * k + 2 + i] = S;
         gnm[(size_t)2 * i] = g->n;
         gnm[(size_t)2 * i + 1] = g->m;
+        max_degree = std::max(max_degree, g->max_degree);
         N += g->n;
         M += g->m;
         S += 2 * g->m;
@@ -1132,6 +1339,7 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
     U.ctx = ctx;
     U.n = N;
     U.m = M;
+    U.max_degree = max_degree;
     BatchDesc *d_desc = nullptr;
     int64_t *d_bases = nullptr;
     long long *d_gnm = nullptr;
@@ -1177,6 +1385,10 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
         pgd_graph_free(&U, U.vrank, (N + 1) * sizeof(int32_t));
         pgd_graph_free(&U, U.adjp_rank, (M + 1) * sizeof(int32_t));
         pgd_graph_free(&U, U.tslot, (S + 1) * sizeof(uint32_t));
+        pgd_graph_free(&U, U.offh, (N + 1) * sizeof(int64_t));
+        pgd_graph_free(&U, U.adjh, (U.nadjh + 1) * sizeof(int32_t));
+        pgd_graph_free(&U, U.toprows, (U.top_words + 1) * sizeof(uint32_t));
+        pgd_graph_free(&U, U.vrec, (N + 1) * 32);
     };
 #define BATCH_TRY(expr)                      \
     do {                                     \
@@ -1228,7 +1440,7 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
     G.gdense = ndense_graphs ? d_gdense : nullptr;
     DenseView dv{(const uint64_t *)bits, d_wbase, d_bases};
     float ms = 0;
-    BATCH_TRY(run_decompose(ctx, G, U.tslot, U.nhubs, &ms, ndense_graphs ? &dv : nullptr));
+    BATCH_TRY(run_decompose(ctx, G, U.tslot, U.nhubs, U.max_degree, &ms, ndense_graphs ? &dv : nullptr));
     std::vector<unsigned long long> h((size_t)k * PGD_NSUMS);
     if (cudaMemcpyAsync(h.data(), gsums, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s)) {
         cleanup();
@@ -1419,7 +1631,13 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     uint32_t *iflag = C.take<uint32_t>(m + 2);
     uint32_t *ipos = C.take<uint32_t>(m + 2);
     int64_t *items = C.take<int64_t>(m + 2);
-    unsigned long long *cache = C.take<unsigned long long>((size_t)nsm * hub_bound);
+    int64_t *offh = C.take<int64_t>(n + 1);
+    int4 *vrec = C.take<int4>(2 * (n + 1));
+    int32_t *adjh = C.take<int32_t>(nnz + 1);
+    HubArgs H;
+    // the maximum degree is not known here: 32-bit counters
+    hub_layout(n, (int32_t)hub_bound, 1 << 30, &H);
+    uint32_t *ghist = H.smem_hist ? nullptr : C.take<uint32_t>((size_t)nsm * H.hstride);
     uint32_t *gbm = in_smem ? nullptr : C.take<uint32_t>((size_t)nsm * nwords);
     void *tmp = C.take<unsigned char>(std::max(tb_scan, tb_sort) + 16);
     if (!C.ok) {
@@ -1462,10 +1680,18 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     NA_CUDA(cudaMemsetAsync(flag + n, 0, sizeof(uint32_t), s));
     NA_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, n + 1, s));
     k_hub_ids<<<grid_for(n), kThreads, 0, s>>>(flag, pos, n, hubid);
+    uint32_t nhubs = 0;
+    NA_CUDA(cudaMemcpyAsync(&nhubs, pos + n, sizeof(nhubs), cudaMemcpyDeviceToHost, s));
+    k_hubnb_flags<<<grid_for(nnz), kThreads, 0, s>>>(d_adj, hubid, nnz, flag);
+    NA_CUDA(cudaMemsetAsync(flag + nnz, 0, sizeof(uint32_t), s));
+    NA_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, nnz + 1, s));
+    k_hubnb_fill<<<grid_for(std::max(nnz, n + 1)), kThreads, 0, s>>>(d_off, d_adj, hubid, flag, pos, n, nnz, offh,
+                                                                      adjh);
     k_rank_keys<<<grid_for(n), kThreads, 0, s>>>(deg, n, rk);
     NA_CUDA(cub::DeviceRadixSort::SortKeys(tmp, tb, rk, rk2, n, 0, 64, s));
     k_rank_scatter<<<grid_for(n), kThreads, 0, s>>>(rk2, n, vrank);
     k_gather_rank<<<grid_for(m), kThreads, 0, s>>>(adjp, vrank, m, adjp_rank);
+    k_vrec<<<grid_for(n), kThreads, 0, s>>>(d_off, offp, deg, vrank, hubid, n, vrec);
 
     DevGraph G;
     G.off = d_off;
@@ -1487,15 +1713,18 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     G.gdense = nullptr;
     G.vrank = vrank;
     G.adjp_rank = adjp_rank;
+    G.offh = offh;
+    G.adjh = adjh;
+    G.toprows = nullptr;   // no rank-bitmap rows here: k4 always scans N+(x)
+    G.vrec = vrec;
+    G.top_r = 0;
     G.anchor_hub = kAnchorHub;
     k_tslot<<<grid_for(32 * m), kThreads, 0, s>>>(G, tslot);
     k_plan_keys<<<grid_for(m), kThreads, 0, s>>>(G, keys, ctr);
     NA_CUDA(cub::DeviceRadixSort::SortKeys(tmp, tb, keys, keys2, m, 0, 64, s));
     k_keys_pos<<<grid_for(m), kThreads, 0, s>>>(keys2, m, posv);
     unsigned long long nh = 0;
-    uint32_t nhubs = 0;
     NA_CUDA(cudaMemcpyAsync(&nh, ctr, sizeof(nh), cudaMemcpyDeviceToHost, s));
-    NA_CUDA(cudaMemcpyAsync(&nhubs, pos + n, sizeof(nhubs), cudaMemcpyDeviceToHost, s));
     NA_CUDA(cudaStreamSynchronize(s));
     int64_t nitems = 0;
     if (nh > 0) {
@@ -1509,21 +1738,21 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
         k_item_fill<<<grid_for(nh), kThreads, 0, s>>>(iflag, ipos, (int64_t)nh, items);
     }
     if (nitems > 0) {
-        const int nh_slots = std::max(1, (int)nhubs);
-        NA_CUDA(cudaMemsetAsync(cache, 0xff, (size_t)nsm * nh_slots * sizeof(unsigned long long), s));
+        // the layout carved above was sized for hub_bound hubs; the
+        // histogram only needs the actual count
+        const size_t smem = hub_layout(n, (int32_t)nhubs, 1 << 30, &H);
+        if (!H.smem_hist && !ghist) {
+            na_msg(err, errlen, "internal: histogram layout changed");
+            return PGD_ECUDA;
+        }
         if (!in_smem) NA_CUDA(cudaMemsetAsync(gbm, 0, (size_t)nsm * nwords * 4, s));
-        const size_t smem = in_smem ? (size_t)nwords * 4 : 0;
         NA_CUDA(cudaFuncSetAttribute(k_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        HubArgs H;
         H.G = G;
         H.hpos = posv;
         H.items = items;
         H.nitems = nitems;
-        H.cache = cache;
-        H.nhubs = nh_slots;
+        H.ghist = ghist;
         H.gbitmap = gbm;
-        H.nwords = nwords;
-        H.smem_bitmap = in_smem ? 1 : 0;
         H.next = ctr + 1;
         k_hub<<<nsm, kHubWarps * 32, smem, s>>>(H);
     }
@@ -1740,7 +1969,7 @@ pgd_status pgd_dev_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pai
         G.gnm = d_gnm;
         G.gdense = ndense_graphs ? d_gdense : nullptr;
         DenseView dv{(const uint64_t *)bits, d_wbase, d_vbase};
-        PB_TRY(run_decompose(ctx, G, U->tslot, U->nhubs, &ms, ndense_graphs ? &dv : nullptr));
+        PB_TRY(run_decompose(ctx, G, U->tslot, U->nhubs, U->max_degree, &ms, ndense_graphs ? &dv : nullptr));
     }
     std::vector<unsigned long long> h((size_t)k * PGD_NSUMS);
     PB_CUDA(cudaMemcpyAsync(h.data(), gsums, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));

@@ -23,7 +23,7 @@ struct pgd_ctx {
     unsigned long long launches = 0;        // kernels of this library launched
     // decomposition thresholds (results never depend on them; pgd_autotune sets them)
     int anchor_hub = 128;    // anchors of degree >= this take the bitmap (block) path
-    int cache_hub = 64;      // W(w,p) cached for neighbours of degree >= this
+    int cache_hub = 64;      // W(w,p) taken from the per-anchor histogram for neighbours of degree >= this
     int dense_max = 2048;    // batched graphs with at most this many vertices use row bitsets
 };
 
@@ -62,9 +62,16 @@ struct pgd_graph {
     bool has_aux = false;
     int64_t *offp = nullptr;          // n+1: degree-oriented lists N+(x)
     int32_t *adjp = nullptr;          // m: neighbours of higher (degree, id)
-    int32_t *hubid = nullptr;         // n: slot in the W cache, -1 if none
+    int32_t *hubid = nullptr;         // n: slot in the W histogram, -1 if none
     int32_t nhubs = 0;
-    int32_t aux_cache_hub = 0;        // cache threshold the hub ids were built with
+    int32_t aux_cache_hub = 0;        // threshold the hub ids were built with
+    int64_t *offh = nullptr;          // n+1: hub-neighbour lists
+    int32_t *adjh = nullptr;          // nadjh: hub ids of each vertex's hub neighbours
+    int64_t nadjh = 0;
+    uint32_t *toprows = nullptr;      // rank-bitmap rows of N+(x) for the top_r highest-ranked x
+    void *vrec = nullptr;             // n * 32 B: per-vertex record for the scans (decompose.cu)
+    int32_t top_r = 0;
+    int64_t top_words = 0;
     int32_t *vrank = nullptr;         // n: rank by (degree desc, id)
     int32_t *adjp_rank = nullptr;     // m: vrank of each adjp entry
     uint32_t *tslot = nullptr;        // 2m: triangle count of each slot's edge

@@ -86,3 +86,45 @@ def test_autotune_keeps_counts():
         o = ol.OracleGraph.from_pairs(s, d, dedup=True).run(micro=False)
         assert (r.totals == o.totals()).all()
     c.close()
+
+
+@pytest.mark.parametrize("case", ["hist16_global", "hist32_global", "bitmap_global"])
+def test_hub_kernel_layouts(case):
+    """k_hub keeps the N(p) bitmap and the W histogram (16-bit counters when
+    the maximum degree is below 65536, else 32-bit) in shared memory when
+    they fit, else in per-CTA global slices; every combination gives the
+    oracle's counts."""
+    c = pgd.Context()
+    n_min = 0
+    if case == "hist16_global":
+        # 120k hubs (every vertex) at 2 B each do not fit in shared memory
+        c.set_thresholds(2, 2)
+        s, d = pgd.barabasi_albert(120000, 6, seed=11)
+    elif case == "hist32_global":
+        # a vertex of degree 70000 forces 32-bit counters; 70k hubs at 4 B
+        c.set_thresholds(2, 2)
+        s0, d0 = pgd.barabasi_albert(70000, 2, seed=13)
+        leaves = np.arange(70000, dtype=np.int32)
+        s = np.concatenate([s0, leaves])
+        d = np.concatenate([d0, np.full(70000, 70000, np.int32)])
+    else:
+        # 2M vertices (mostly isolated): the bitmap (n bits) goes to global memory
+        s, d = pgd.rmat(12, 16, seed=12)
+        n_min = 2_000_000
+    g = c.graph_from_edges(s, d, n_min=n_min)
+    og = ol.OracleGraph.from_pairs(s, d, n_min=n_min, dedup=True)
+    deg = np.diff(og.csr()[0])
+    if case == "hist16_global":
+        assert deg.max() < 65536 and (deg >= 2).sum() * 2 + len(deg) / 8 > 188 * 1024
+    elif case == "hist32_global":
+        assert deg.max() >= 65536 and (deg >= 2).sum() * 4 + len(deg) / 8 > 188 * 1024
+    else:
+        assert len(deg) / 8 > 160 * 1024
+    r = g.decompose(micro=True)
+    o = og.run()
+    assert (r.totals == o.totals()).all()
+    assert (r.sums == o.sums()).all()
+    a, b, cols = g.micro()
+    x, y, z = o.micro()
+    assert (cols == z).all()
+    c.close()
