@@ -165,11 +165,12 @@ extern "C" pgd_status pgd_graph_destroy(pgd_graph *g) {
     pgd_graph_free(g, g->hubid, (g->n + 1) * sizeof(int32_t));
     pgd_graph_free(g, g->vrank, (g->n + 1) * sizeof(int32_t));
     pgd_graph_free(g, g->adjp_rank, (g->m + 1) * sizeof(int32_t));
-    pgd_graph_free(g, g->tslot, (2 * g->m + 1) * sizeof(uint32_t));
+    pgd_graph_free(g, g->slot, (2 * g->m + 1) * 16);
     pgd_graph_free(g, g->offh, (g->n + 1) * sizeof(int64_t));
     pgd_graph_free(g, g->adjh, (g->nadjh + 1) * sizeof(int32_t));
     pgd_graph_free(g, g->toprows, (g->top_words + 1) * sizeof(uint32_t));
     pgd_graph_free(g, g->vrec, (g->n + 1) * 32);
+    pgd_graph_free(g, g->adj_rank, (2 * g->m + 1) * sizeof(int32_t));
     // whatever is left (partial builds) is returned to the budget as well
     g->ctx->resident -= g->bytes;
     cudaStreamSynchronize(g->ctx->stream);

@@ -61,7 +61,6 @@ constexpr int kLightStageMax = 256;      // largest warp/block threshold the lig
 constexpr int kChunk = 2048;             // edges of one anchor per CTA work item (target)
 constexpr int kMaxChunks = 8;            // ... but an anchor is split into at most this many items, since
                                          // every item rebuilds the anchor's bitmap and W histogram
-constexpr int kMaxSmemBitmap = 150 * 1024;
 constexpr int kMaxDynSmem = 156 * 1024;  // k_hub dynamic shared memory: bitmap, then the W histogram
 constexpr int kRankBits = 16384;         // T members of degree rank below this are marked in a per-warp bitmap;
                                          // vertices of rank below this get a rank-bitmap row of N+(x)
@@ -80,7 +79,8 @@ struct DevGraph {
     const int64_t *offp;
     const int32_t *adjp;
     const int32_t *hubid;
-    const uint32_t *tslot;
+    const int32_t *adj_rank;    // vrank of each adjacency entry
+    const int4 *slot;           // per adjacency slot: {w, vrank(w) | row flag << 31, hubid(w), t of the slot's edge}
     const int32_t *ev;
     const int32_t *eu;
     const int32_t *order;
@@ -205,6 +205,18 @@ __global__ void k_vrec(const int64_t *off, const int64_t *offp, const int32_t *d
     }
 }
 
+// Per adjacency slot j (entry w = adj[j]): {w, vrank(w), hubid(w), t}, with
+// bit 31 of the rank set when |N+(w) n T| is taken from w's rank-bitmap row
+// (rank below top_r and the row shorter than N+(w)).  t is filled by k_tslot.
+__global__ void k_slot_fill(const int32_t *adj, const int32_t *vrank, const int32_t *hubid, const int64_t *offp,
+                            int64_t nnz, int top_r, int4 *slot) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nnz; j += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t w = adj[j], r = vrank[w];
+        const bool row = r < top_r && (r >> 5) + 1 < (int)(offp[w + 1] - offp[w]);
+        slot[j] = make_int4(w, (int)((uint32_t)r | (row ? 0x80000000u : 0u)), hubid[w], 0);
+    }
+}
+
 __global__ void k_hub_flags(const int32_t *deg, int64_t n, int cache_hub, uint32_t *flag) {
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
         flag[v] = deg[v] >= cache_hub ? 1u : 0u;
@@ -215,9 +227,9 @@ __global__ void k_hub_ids(const uint32_t *flag, const uint32_t *pos, int64_t n, 
         hubid[v] = flag[v] ? (int32_t)pos[v] : -1;
 }
 
-// t of every edge, written to both of its CSR slots.  One warp per edge:
+// t of every edge, written to both of its CSR slots (the slot records' last field).  One warp per edge:
 // the shorter list's entries are searched in the longer one.
-__global__ void k_tslot(DevGraph G, uint32_t *tslot) {
+__global__ void k_tslot(DevGraph G, int4 *slot) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t id = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; id < G.m; id += nw) {
@@ -232,20 +244,22 @@ __global__ void k_tslot(DevGraph G, uint32_t *tslot) {
         unsigned long long t = 0;
         for (int i = lane; i < ds; i += 32) t += pgd_contains(Nl, dl, __ldg(Ns + i)) ? 1 : 0;
         t = pgd_warp_sum(t);
-        if (lane == 0) tslot[G.off[a] + pgd_lower_bound(G.adj + G.off[a], da, b)] = (uint32_t)t;
-        if (lane == 1) tslot[G.off[b] + pgd_lower_bound(G.adj + G.off[b], db, a)] = (uint32_t)t;
+        if (lane == 0) slot[G.off[a] + pgd_lower_bound(G.adj + G.off[a], da, b)].w = (int)t;
+        if (lane == 1) slot[G.off[b] + pgd_lower_bound(G.adj + G.off[b], db, a)].w = (int)t;
     }
 }
 
 // ---------------------------------------------------------------------------
 // work plan: hub-anchored edges grouped by anchor, light edges listed
 
-// key = (rank(anchor) << 32 | position) for hub-anchored edges,
-// (~0 << 32 | position) for the rest, so one sort groups the first, highest
-// degree anchors first (the largest work items are handed out first), and
-// lists the second in order.  Dense-graph edges (batches only) get
+// Sort keys of the work plan, with the E_ordered position as the value.
+// Hub-anchored edges: (rank(anchor) << 32 | position), so one sort groups
+// them by anchor, highest-degree anchors first (the largest work items are
+// handed out first).  (Heaviest-edge-first within an anchor shortens the
+// items' tails but was measured slower: all warps then gather hub lists at
+// once.)  The rest: (~0 << 32 | position), dense-graph edges (batches only)
 // 0xfffffffe, so the sorted order is [hub-anchored, by anchor][dense][light].
-__global__ void k_plan_keys(DevGraph G, uint64_t *keys, unsigned long long *counts) {
+__global__ void k_plan_keys(DevGraph G, uint64_t *keys, int32_t *vals, unsigned long long *counts) {
     unsigned long long hubs = 0, dense = 0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < G.m; e += (int64_t)gridDim.x * blockDim.x) {
         const int32_t id = G.order[e];
@@ -255,6 +269,7 @@ __global__ void k_plan_keys(DevGraph G, uint64_t *keys, unsigned long long *coun
         const bool hub = !d && G.deg[p] >= G.anchor_hub;
         const uint32_t hi = d ? 0xfffffffeu : (hub ? (uint32_t)G.vrank[p] : 0xffffffffu);
         keys[e] = ((uint64_t)hi << 32) | (uint32_t)e;
+        vals[e] = (int32_t)e;
         hubs += hub;
         dense += d;
     }
@@ -290,16 +305,24 @@ __global__ void k_item_flags(const uint64_t *keys, int64_t nh, uint32_t *flag) {
     }
 }
 
+// Per hub-anchored plan position i: {E_ordered position e, the non-anchor
+// endpoint q}, so that k_hub starts an edge with one load instead of a chain
+// of four (position -> edge id -> endpoints -> q).
+__global__ void k_hub_recs(DevGraph G, const int32_t *hpos, int64_t nh, int2 *hrec) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nh; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t e = hpos[i];
+        const int32_t id = G.order[e];
+        const int32_t v = G.ev[id], u = G.eu[id];
+        hrec[i] = make_int2(e, ranks_above(v, u, G.deg) ? u : v);
+    }
+}
+
 __global__ void k_item_fill(const uint32_t *flag, const uint32_t *pos, int64_t nh, int64_t *items) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nh; i += (int64_t)gridDim.x * blockDim.x)
         if (flag[i]) items[pos[i]] = i;
     if (blockIdx.x == 0 && threadIdx.x == 0) items[pos[nh]] = nh;
 }
 
-__global__ void k_keys_pos(const uint64_t *keys, int64_t n, int32_t *posv) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        posv[i] = (int32_t)(uint32_t)(keys[i] & 0xffffffffu);
-}
 
 // ---------------------------------------------------------------------------
 // shared per-edge epilogue
@@ -316,10 +339,9 @@ __device__ __forceinline__ void flush_graph(const DevGraph &G, unsigned long lon
 // Closed forms, sums and the per-edge row of one edge.  Batched runs keep
 // the sums of the current graph in acc and flush them when the warp moves
 // on to another graph (cur_g).
-__device__ __forceinline__ void edge_epilogue(const DevGraph &G, unsigned long long *acc, int &cur_g, int64_t e,
-                                              int32_t v, int32_t u, unsigned long long t, unsigned long long k4,
-                                              unsigned long long c4, int lane) {
-    const long long dv = G.deg[v], du = G.deg[u];
+__device__ __forceinline__ void edge_epilogue_d(const DevGraph &G, unsigned long long *acc, int &cur_g, int64_t e,
+                                                long long dv, long long du, unsigned long long t,
+                                                unsigned long long k4, unsigned long long c4, int lane) {
     long long n = G.n, m = G.m;
     if (G.egraph) {
         const int g = G.egraph[e];
@@ -336,6 +358,13 @@ __device__ __forceinline__ void edge_epilogue(const DevGraph &G, unsigned long l
         acc[4] += c4;
     }
     if (G.micro && lane < PGD_NMICRO) G.micro[e * PGD_NMICRO + lane] = pgd_micro_col(lane, dv, du, t, k4, c4);
+}
+
+// The closed forms are symmetric in the two endpoints: only their degrees matter.
+__device__ __forceinline__ void edge_epilogue(const DevGraph &G, unsigned long long *acc, int &cur_g, int64_t e,
+                                              int32_t v, int32_t u, unsigned long long t, unsigned long long k4,
+                                              unsigned long long c4, int lane) {
+    edge_epilogue_d(G, acc, cur_g, e, G.deg[v], G.deg[u], t, k4, c4, lane);
 }
 
 __device__ __forceinline__ void block_flush(const DevGraph &G, unsigned long long *acc, int cur_g,
@@ -369,18 +398,37 @@ __device__ __forceinline__ int owner_of(int incl, int it) {
     return lo;
 }
 
-__device__ __forceinline__ bool bit_of(const uint32_t *bm, int32_t x) { return (bm[x >> 5] >> (x & 31)) & 1u; }
+
+// N(p) as a bitmap over degree ranks: ranks below `split` in shared memory,
+// the rest in this CTA's global slice.  Queries are weighted by degree, so
+// almost all of them land in the shared part.
+struct RankBits {
+    uint32_t *s;       // shared words (ranks < split)
+    uint32_t *g;       // global slice (indexed by rank >> 5; only ranks >= split are used)
+    int32_t split;     // multiple of 32
+    __device__ __forceinline__ bool test(int32_t r) const {
+        return r < split ? (s[r >> 5] >> (r & 31)) & 1u : (__ldcg(g + (r >> 5)) >> (r & 31)) & 1u;
+    }
+    __device__ __forceinline__ void set(int32_t r) const {
+        if (r < split) atomicOr(s + (r >> 5), 1u << (r & 31));
+        else atomicOr(g + (r >> 5), 1u << (r & 31));
+    }
+    __device__ __forceinline__ void clear_word(int32_t r) const {
+        if (r < split) s[r >> 5] = 0;
+        else g[r >> 5] = 0;
+    }
+};
 
 // ---------------------------------------------------------------------------
 // Hub anchors: one CTA per (anchor, chunk of its edges).
 //
-// Per work item: (1) N(p) goes into the bitmap and, in the same pass, the
+// Per work item: (1) N(p) goes into the rank bitmap and, in the same pass, the
 // hub-neighbour lists of N(p) are histogrammed: afterwards hist[h] =
 // |N(w_h) n N(p)| = W(w_h, p) for every hub w_h, whatever q needs it.
 // (2) The chunk's edges are decomposed, one warp each, fetched dynamically.
 // Per edge the warp first collects T (marked by degree rank in a per-warp
 // bitmap), t, sum t(x,q) and the W's of hub neighbours, then scans what is
-// left: N(w) of non-hub w in S_q (W by bit tests in the N(p) bitmap) and, for
+// left: N(w) of non-hub w in S_q (W by bit tests of its entries' ranks) and, for
 // k4, |N+(x) n T| of x in T, either from x's oriented list or, for the
 // highest-ranked x, as AND + popc of x's rank-bitmap row with the T bitmap.
 // Lists of 64 or more entries are read warp-cooperatively; shorter ones are
@@ -392,6 +440,7 @@ __device__ __forceinline__ bool bit_of(const uint32_t *bm, int32_t x) { return (
 struct HubArgs {
     DevGraph G;
     const int32_t *hpos;      // E_ordered positions of hub-anchored edges, grouped by anchor
+    const int2 *hrec;         // per position: {E_ordered position, non-anchor endpoint q}
     const int64_t *items;     // chunk starts into hpos, nitems+1 entries
     int64_t nitems;
     uint32_t *ghist;          // per CTA histogram slices (hstride words each) when not in shared memory
@@ -399,21 +448,22 @@ struct HubArgs {
     int64_t hstride;
     int smem_hist;
     int hist16;               // two 16-bit counters per word (every W < 65536: max degree below that)
-    uint32_t *gbitmap;        // per CTA bitmap slices when not in shared memory
+    uint32_t *gbitmap;        // per CTA rank-bitmap slices (nwords each) when split < n
     int64_t nwords;
-    int smem_bitmap;
+    int32_t split;            // ranks below this are kept in shared memory
     unsigned long long *next;
 };
 
-// |{x in L[0..len) : bit(x)}|, warp-cooperative, 4 loads in flight per lane.
-__device__ __forceinline__ unsigned count_bits(const uint32_t *bm, const int32_t *L, int len, int lane) {
+// |{r in L[0..len) : r in N(p)}| for a list of ranks, warp-cooperative,
+// 4 loads in flight per lane.
+__device__ __forceinline__ unsigned count_bits(const RankBits &bm, const int32_t *L, int len, int lane) {
     unsigned c = 0;
     int i = lane;
     for (; i + 96 < len; i += 128) {
         const int32_t x0 = __ldg(L + i), x1 = __ldg(L + i + 32), x2 = __ldg(L + i + 64), x3 = __ldg(L + i + 96);
-        c += bit_of(bm, x0) + bit_of(bm, x1) + bit_of(bm, x2) + bit_of(bm, x3);
+        c += bm.test(x0) + bm.test(x1) + bm.test(x2) + bm.test(x3);
     }
-    for (; i < len; i += 32) c += bit_of(bm, __ldg(L + i));
+    for (; i < len; i += 32) c += bm.test(__ldg(L + i));
     return c;
 }
 
@@ -428,12 +478,12 @@ __device__ __forceinline__ unsigned row_and_count(const uint32_t *row, const uin
 
 // y in T = N(p) n N(q).  Almost every y tested is a high-degree vertex, so
 // T's members of degree rank < kRankBits are marked in a per-warp bitmap and
-// the test is one shared-memory bit; other y fall back to the p bitmap and a
-// search of N(q).
-__device__ __forceinline__ bool in_t(const uint32_t *Rw, const uint32_t *bm, const int32_t *Nq, int dq, int32_t y,
+// the test is one shared-memory bit; other y fall back to the N(p) bitmap and
+// a search of N(q).
+__device__ __forceinline__ bool in_t(const uint32_t *Rw, const RankBits &bm, const int32_t *Nq, int dq, int32_t y,
                                      int32_t ry) {
     if (ry < kRankBits) return (Rw[ry >> 5] >> (ry & 31)) & 1u;
-    return bit_of(bm, y) && pgd_contains(Nq, dq, y);
+    return bm.test(ry) && pgd_contains(Nq, dq, y);
 }
 
 // Histogram of the hub ids in the lists of the 32 vertices the warp holds
@@ -475,29 +525,32 @@ __device__ __forceinline__ int hist_lists(const int32_t *list, int len, int lane
 __device__ __forceinline__ int64_t rec_off(const int4 &ra) { return (int64_t)(((uint64_t)(uint32_t)ra.y << 32) | (uint32_t)ra.x); }
 __device__ __forceinline__ int64_t rec_offp(const int4 &ra) { return (int64_t)(((uint64_t)(uint32_t)ra.w << 32) | (uint32_t)ra.z); }
 
-// What pass 2 scans for neighbour w of q (records ra, rb): for w in T, N+(w)
-// as a list (kind 1) or a rank-bitmap row (kind 2); for a non-hub w outside
-// N(p), N(w) (kind 0); nothing otherwise (len 0).
-__device__ __forceinline__ void plan_entry(const DevGraph &G, bool inT, const int4 &ra, const int4 &rb, int &len,
-                                           int &kind, const int32_t *&list, const int32_t *&rlist) {
+// What pass 2 scans for neighbour w of q (slot record sr): for w in T, N+(w)
+// as a rank-bitmap row (kind 2, from the rank alone) or as a list (kind 1);
+// for a non-hub w outside N(p), N(w) (kind 0); nothing otherwise (len 0).
+// Lists need w's offsets: one 32-byte vertex record.
+__device__ __forceinline__ void plan_entry(const DevGraph &G, bool inT, const int4 &sr, int &len, int &kind,
+                                           const int32_t *&list, const int32_t *&rlist) {
+    const int32_t w = sr.x;
     if (inT) {
-        const int32_t r = rb.z;
-        const int dplus = rb.y, words = (r >> 5) + 1;
-        if (r < G.top_r && words < dplus) {
+        const int32_t r = sr.y & 0x7fffffff;
+        if (sr.y < 0) {
             kind = 2;
-            len = words;
+            len = (r >> 5) + 1;
             list = (const int32_t *)(G.toprows + top_row_base(r));
         } else {
+            const int4 ra = __ldg(G.vrec + 2 * (int64_t)w), rb = __ldg(G.vrec + 2 * (int64_t)w + 1);
             const int64_t o = rec_offp(ra);
             kind = 1;
-            len = dplus;
+            len = rb.y;
             list = G.adjp + o;
             rlist = G.adjp_rank + o;
         }
-    } else if (rb.w < 0) {
+    } else if (sr.z < 0) {
+        const int4 ra = __ldg(G.vrec + 2 * (int64_t)w), rb = __ldg(G.vrec + 2 * (int64_t)w + 1);
         kind = 0;
         len = rb.x;
-        list = G.adj + rec_off(ra);
+        list = G.adj_rank + rec_off(ra);   // ranks: tested against the N(p) rank bitmap
     }
 }
 
@@ -512,11 +565,14 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     uint32_t *Rw = s_R[wid];
     for (int i = lane; i < kRankBits / 32; i += 32) Rw[i] = 0;
-    uint32_t *bm = A.smem_bitmap ? s_dyn : A.gbitmap + (int64_t)blockIdx.x * A.nwords;
-    // histogram: shared (after the bitmap, 16-byte aligned) or this CTA's global slice
-    uint32_t *sh_hist = s_dyn + (A.smem_bitmap ? ((A.nwords + 3) & ~(int64_t)3) : 0);
-    uint32_t *gl_hist = A.ghist + (int64_t)blockIdx.x * A.hstride;
     const bool smem_hist = A.smem_hist != 0;
+    // dynamic shared memory: [histogram (when shared)][rank bitmap, ranks < split]
+    uint32_t *sh_hist = s_dyn;
+    uint32_t *gl_hist = A.ghist + (int64_t)blockIdx.x * A.hstride;
+    RankBits bm;
+    bm.s = s_dyn + (smem_hist ? A.hstride : 0);
+    bm.g = A.gbitmap ? A.gbitmap + (int64_t)blockIdx.x * A.nwords : nullptr;
+    bm.split = A.split;
     const bool h16 = A.hist16 != 0;
     // this warp's partial sums live in shared memory (lane 0 updates them),
     // which keeps 30 registers free for the gathers
@@ -528,8 +584,7 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
     auto hinc = [h16](int32_t h) { return h16 ? (1u << ((h & 1) << 4)) : 1u; };
     auto hval = [h16](uint32_t word, int32_t h) { return h16 ? ((word >> ((h & 1) << 4)) & 0xffffu) : word; };
     int cur_g = -1;
-    if (A.smem_bitmap)
-        for (int64_t i = threadIdx.x; i < A.nwords; i += blockDim.x) bm[i] = 0;
+    for (int i = threadIdx.x; i < (A.split >> 5); i += blockDim.x) bm.s[i] = 0;
     {
         uint4 *h4 = (uint4 *)(smem_hist ? sh_hist : gl_hist);
         for (int i = threadIdx.x; i < nh4; i += blockDim.x) h4[i] = make_uint4(0, 0, 0, 0);
@@ -555,6 +610,7 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
         }
         const int dp = G.deg[p];
         const int32_t *Np = G.adj + G.off[p];
+        const int32_t *Rp = G.adj_rank + G.off[p];
 
         // ---- (1) N(p) bitmap and the W histogram --------------------------
         {
@@ -565,7 +621,7 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                 const int32_t *list = nullptr;
                 if (j < dp) {
                     const int32_t x = __ldg(Np + j);
-                    atomicOr(bm + (x >> 5), 1u << (x & 31));
+                    bm.set(__ldg(Rp + j));
                     const int64_t o = G.offh[x];
                     len = (int)(G.offh[x + 1] - o);
                     list = G.adjh + o;
@@ -580,17 +636,22 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
         __syncthreads();
 
         // ---- (2) the chunk's edges ---------------------------------------
-        while (true) {
-            int k = 0;
-            if (lane == 0) k = atomicAdd(&s_enext, 1);
-            k = __shfl_sync(0xffffffffu, k, 0);
-            if (k >= nedge) break;
-            const int64_t e = A.hpos[start + k];
-            const int32_t id = G.order[e];
-            const int32_t v = G.ev[id], u = G.eu[id];
-            const int32_t q = (v == p) ? u : v;
-            const int dq = G.deg[q];
-            const int64_t offq = G.off[q];
+        // fetched one ahead: the next edge's record is in flight while the
+        // current edge is decomposed
+        int kc = 0;
+        if (lane == 0) kc = atomicAdd(&s_enext, 1);
+        kc = __shfl_sync(0xffffffffu, kc, 0);
+        int2 rc = kc < nedge ? __ldg(A.hrec + start + kc) : make_int2(0, 0);
+        while (kc < nedge) {
+            int kn = 0;
+            if (lane == 0) kn = atomicAdd(&s_enext, 1);
+            kn = __shfl_sync(0xffffffffu, kn, 0);
+            const int2 rn = kn < nedge ? __ldg(A.hrec + start + kn) : make_int2(0, 0);
+            const int64_t e = rc.x;
+            const int32_t q = rc.y;
+            const int4 qa = __ldg(G.vrec + 2 * (int64_t)q), qb = __ldg(G.vrec + 2 * (int64_t)q + 1);
+            const int dq = qb.x;
+            const int64_t offq = rec_off(qa);
             const int32_t *Nq = G.adj + offq;
             // pass 1: T (rank bitmap), t, sum of t(x,q) over T, W's of hubs;
             // for q of degree <= 32 also what pass 2 scans, kept in registers
@@ -598,27 +659,29 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
             unsigned long long sumtq = 0, sumW = 0, k4 = 0;
             int len0 = 0, kind0 = 0;
             const int32_t *list0 = nullptr, *rlist0 = nullptr;
-            for (int base = 0; base < dq; base += 32) {
-                const int j = base + lane;
-                bool inT = false;
-                if (j < dq) {
-                    const int32_t w = __ldg(Nq + j);
-                    if (w != p) {
-                        const int4 ra = __ldg(G.vrec + 2 * (int64_t)w), rb = __ldg(G.vrec + 2 * (int64_t)w + 1);
-                        const uint32_t tq = __ldg(G.tslot + offq + j);
-                        inT = bit_of(bm, w);
+            for (int base = 0; base < dq; base += 64) {
+                const int j0 = base + lane, j1 = base + 32 + lane;
+                const int4 none = make_int4(p, 0, -1, 0);
+                const int4 s0 = j0 < dq ? __ldg(G.slot + offq + j0) : none;
+                const int4 s1 = j1 < dq ? __ldg(G.slot + offq + j1) : none;
+#pragma unroll
+                for (int h2 = 0; h2 < 2; h2++) {
+                    const int4 sr = h2 ? s1 : s0;
+                    bool inT = false;
+                    if (sr.x != p) {
+                        inT = bm.test(sr.y & 0x7fffffff);
                         if (inT) {
-                            sumtq += tq;
-                            const int32_t r = rb.z;
+                            sumtq += (uint32_t)sr.w;
+                            const int32_t r = sr.y & 0x7fffffff;
                             if (r < kRankBits) atomicOr(Rw + (r >> 5), 1u << (r & 31));
                         } else {
-                            const int32_t h = rb.w;
+                            const int32_t h = sr.z;
                             if (h >= 0) sumW += hval(smem_hist ? sh_hist[hw(h)] : __ldcg(gl_hist + hw(h)), h);
                         }
-                        if (dq <= 32) plan_entry(G, inT, ra, rb, len0, kind0, list0, rlist0);
+                        if (dq <= 32 && h2 == 0) plan_entry(G, inT, sr, len0, kind0, list0, rlist0);
                     }
+                    t += __popc(__ballot_sync(0xffffffffu, inT));
                 }
-                t += __popc(__ballot_sync(0xffffffffu, inT));
             }
             __syncwarp();
             // pass 2: N(w) of non-hub w in S_q (kind 0), N+(x) of x in T as a
@@ -633,11 +696,8 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                     kind = 0;
                     list = rlist = nullptr;
                     if (j < dq) {
-                        const int32_t w = __ldg(Nq + j);
-                        if (w != p) {
-                            const int4 ra = __ldg(G.vrec + 2 * (int64_t)w), rb = __ldg(G.vrec + 2 * (int64_t)w + 1);
-                            plan_entry(G, bit_of(bm, w), ra, rb, len, kind, list, rlist);
-                        }
+                        const int4 sr = __ldg(G.slot + offq + j);
+                        if (sr.x != p) plan_entry(G, bm.test(sr.y & 0x7fffffff), sr, len, kind, list, rlist);
                     }
                 }
                 // long lists (>= 64 entries): one at a time, warp-cooperative
@@ -684,12 +744,12 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                     const int32_t rA = (vA && okA == 1) ? __ldg(orA + idxA) : 0;
                     const int32_t rB = (vB && okB == 1) ? __ldg(orB + idxB) : 0;
                     if (vA) {
-                        if (okA == 0) sumW += bit_of(bm, xA);
+                        if (okA == 0) sumW += bm.test(xA);
                         else if (okA == 2) k4 += __popc((uint32_t)xA & Rw[idxA]);
                         else k4 += in_t(Rw, bm, Nq, dq, xA, rA) ? 1 : 0;
                     }
                     if (vB) {
-                        if (okB == 0) sumW += bit_of(bm, xB);
+                        if (okB == 0) sumW += bm.test(xB);
                         else if (okB == 2) k4 += __popc((uint32_t)xB & Rw[idxB]);
                         else k4 += in_t(Rw, bm, Nq, dq, xB, rB) ? 1 : 0;
                     }
@@ -700,13 +760,15 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
             k4 = pgd_warp_sum(k4);
             const long long c4 = (long long)sumW - ((long long)dq - (long long)t - 1) - (long long)sumtq +
                                  2 * (long long)k4 + (long long)t;
-            edge_epilogue(G, acc, cur_g, e, v, u, t, k4, (unsigned long long)c4, lane);
+            edge_epilogue_d(G, acc, cur_g, e, dp, dq, t, k4, (unsigned long long)c4, lane);
             __syncwarp();
             for (int i = lane; i < kRankBits / 32; i += 32) Rw[i] = 0;
             __syncwarp();
+            kc = kn;
+            rc = rn;
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < dp; i += blockDim.x) bm[__ldg(Np + i) >> 5] = 0;
+        for (int i = threadIdx.x; i < dp; i += blockDim.x) bm.clear_word(__ldg(Rp + i));
         if (s_hcount * 4 >= (unsigned long long)A.nhubs) {
             uint4 *h4 = (uint4 *)(smem_hist ? sh_hist : gl_hist);
             for (int i = threadIdx.x; i < nh4; i += blockDim.x) h4[i] = make_uint4(0, 0, 0, 0);
@@ -794,7 +856,7 @@ __global__ void __launch_bounds__(kLightWarps * 32) k_light(LightArgs A) {
                     const int pos = pgd_lower_bound(np_s, dp, w);
                     if (pos < dp && np_s[pos] == w) {     // w in T
                         t++;
-                        sumtq += G.tslot[offq + j];
+                        sumtq += (uint32_t)G.slot[offq + j].w;
                         kind = 1;
                         const int64_t o = G.offp[w];
                         len = (int)(G.offp[w + 1] - o);
@@ -966,7 +1028,8 @@ static pgd_status build_aux(pgd_graph *g) {
         if ((st = pgd_graph_alloc(g, (void **)&g->vrank, (n + 1) * sizeof(int32_t)))) return st;
         if ((st = pgd_graph_alloc(g, (void **)&g->adjp_rank, (g->m + 1) * sizeof(int32_t)))) return st;
         if ((st = pgd_graph_alloc(g, (void **)&g->hubid, (n + 1) * sizeof(int32_t)))) return st;
-        if ((st = pgd_graph_alloc(g, (void **)&g->tslot, (nnz + 1) * sizeof(uint32_t)))) return st;
+        if ((st = pgd_graph_alloc(g, (void **)&g->slot, (nnz + 1) * sizeof(int4)))) return st;
+        if ((st = pgd_graph_alloc(g, (void **)&g->adj_rank, (nnz + 1) * sizeof(int32_t)))) return st;
         if ((st = pgd_graph_alloc(g, (void **)&g->offh, (n + 1) * sizeof(int64_t)))) return st;
         if ((st = pgd_graph_alloc(g, (void **)&g->vrec, (n + 1) * 32))) return st;
         g->top_r = (int32_t)std::min<int64_t>(n, kRankBits);
@@ -1035,13 +1098,19 @@ static pgd_status build_aux(pgd_graph *g) {
             pgd_tmp_free(ctx, tmp);
             PGD_LAUNCH(ctx, k_rank_scatter, grid_for(n), kThreads, 0, rk2, n, g->vrank);
         }
-        if (g->m > 0) PGD_LAUNCH(ctx, k_gather_rank, grid_for(g->m), kThreads, 0, g->adjp, g->vrank, g->m, g->adjp_rank);
+        if (g->m > 0) {
+            PGD_LAUNCH(ctx, k_gather_rank, grid_for(g->m), kThreads, 0, g->adjp, g->vrank, g->m, g->adjp_rank);
+            PGD_LAUNCH(ctx, k_gather_rank, grid_for(nnz), kThreads, 0, g->adj, g->vrank, nnz, g->adj_rank);
+        }
         pgd_tmp_free(ctx, rk);
         pgd_tmp_free(ctx, rk2);
     }
     if (n > 0)
         PGD_LAUNCH(ctx, k_vrec, grid_for(n), kThreads, 0, g->off, g->offp, g->deg, g->vrank, g->hubid, n,
                    (int4 *)g->vrec);
+    if (nnz > 0)
+        PGD_LAUNCH(ctx, k_slot_fill, grid_for(nnz), kThreads, 0, g->adj, g->vrank, g->hubid, g->offp, nnz, g->top_r,
+                   (int4 *)g->slot);
     // rank-bitmap rows of the highest-ranked vertices (ranks do not depend on
     // the thresholds, so a rebuild for new thresholds recomputes the same rows)
     PGD_CUDA(ctx, cudaMemsetAsync(g->toprows, 0, (g->top_words + 1) * sizeof(uint32_t), s));
@@ -1067,7 +1136,7 @@ static DevGraph dev_view(pgd_graph *g, bool micro) {
     G.offp = g->offp;
     G.adjp = g->adjp;
     G.hubid = g->hubid;
-    G.tslot = g->tslot;
+    G.slot = (const int4 *)g->slot;
     G.ev = g->ev;
     G.eu = g->eu;
     G.order = g->order;
@@ -1080,6 +1149,7 @@ static DevGraph dev_view(pgd_graph *g, bool micro) {
     G.gdense = nullptr;
     G.vrank = g->vrank;
     G.adjp_rank = g->adjp_rank;
+    G.adj_rank = g->adj_rank;
     G.offh = g->offh;
     G.adjh = g->adjh;
     G.toprows = g->toprows;
@@ -1097,22 +1167,24 @@ struct DenseView {
     const int64_t *vbase;
 };
 
-// Where k_hub keeps the N(p) bitmap and the W histogram: shared memory when
-// they fit (the bitmap first), else per-CTA global slices.  Fills the layout
-// fields of H and returns the dynamic shared memory size.
+// Where k_hub keeps the W histogram and the N(p) rank bitmap: the histogram
+// (atomics) in shared memory when it fits, then as many bitmap ranks as the
+// remaining shared memory holds; per-CTA global slices for the rest.  Fills
+// the layout fields of H and returns the dynamic shared memory size.
 static size_t hub_layout(int64_t n, int32_t nhubs, int32_t max_degree, HubArgs *H) {
     H->nwords = (n + 31) / 32;
     H->nhubs = nhubs;
     H->hist16 = max_degree < 65536 ? 1 : 0;
     const int64_t hwords = H->hist16 ? ((int64_t)nhubs + 1) / 2 : (int64_t)nhubs;
     H->hstride = std::max<int64_t>(4, (hwords + 3) & ~(int64_t)3);
-    H->smem_bitmap = H->nwords * 4 <= kMaxSmemBitmap ? 1 : 0;
-    const int64_t bm_bytes = H->smem_bitmap ? ((H->nwords + 3) & ~(int64_t)3) * 4 : 0;
-    H->smem_hist = bm_bytes + H->hstride * 4 <= kMaxDynSmem ? 1 : 0;
-    return (size_t)(bm_bytes + (H->smem_hist ? H->hstride * 4 : 0));
+    H->smem_hist = H->hstride * 4 <= kMaxDynSmem ? 1 : 0;
+    const int64_t rem_words = kMaxDynSmem / 4 - (H->smem_hist ? H->hstride : 0);
+    const int64_t bm_words = std::min<int64_t>(H->nwords, rem_words);
+    H->split = (int32_t)std::min<int64_t>(bm_words * 32, 0x7fffffe0);
+    return (size_t)((H->smem_hist ? H->hstride : 0) + bm_words) * 4;
 }
 
-static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, uint32_t *tslot, int32_t nhubs, int32_t max_degree,
+static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int32_t nhubs, int32_t max_degree,
                                 float *ms, const DenseView *dense = nullptr) {
     cudaStream_t s = ctx->stream;
     pgd_status st;
@@ -1120,27 +1192,28 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, uint32_t *tslot
     *ms = 0;
     if (m == 0) return PGD_OK;
     uint64_t *keys = nullptr, *keys2 = nullptr;
-    int32_t *posv = nullptr;
+    int32_t *posv = nullptr, *vals = nullptr;
     uint32_t *flag = nullptr, *fpos = nullptr;
     int64_t *items = nullptr;
     uint32_t *ghist = nullptr;
     uint32_t *gbm = nullptr;
+    int2 *hrec = nullptr;
     if ((st = pgd_tmp_alloc(ctx, (void **)&keys, m * sizeof(uint64_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&keys2, m * sizeof(uint64_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&posv, m * sizeof(int32_t)))) return st;
+    if ((st = pgd_tmp_alloc(ctx, (void **)&vals, m * sizeof(int32_t)))) return st;
     // [0] hub edges, [1] hub item counter, [2] light counter, [3] dense edges, [4] dense counter
     unsigned long long *ctr = ctx->d_ctr;
     PGD_CUDA(ctx, cudaMemsetAsync(ctr, 0, 8 * sizeof(unsigned long long), s));
     PGD_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
-    PGD_LAUNCH(ctx, k_tslot, grid_for(32 * m), kThreads, 0, G, tslot);
-    PGD_LAUNCH(ctx, k_plan_keys, grid_for(m), kThreads, 0, G, keys, ctr);
+    PGD_LAUNCH(ctx, k_tslot, grid_for(32 * m), kThreads, 0, G, slot);
+    PGD_LAUNCH(ctx, k_plan_keys, grid_for(m), kThreads, 0, G, keys, vals, ctr);
     size_t tb = 0;
     void *tmp = nullptr;
-    cub::DeviceRadixSort::SortKeys(nullptr, tb, keys, keys2, m, 0, 64, s);
+    cub::DeviceRadixSort::SortPairs(nullptr, tb, keys, keys2, vals, posv, m, 0, 64, s);
     if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
-    cub::DeviceRadixSort::SortKeys(tmp, tb, keys, keys2, m, 0, 64, s);
+    cub::DeviceRadixSort::SortPairs(tmp, tb, keys, keys2, vals, posv, m, 0, 64, s);
     pgd_tmp_free(ctx, tmp);
-    PGD_LAUNCH(ctx, k_keys_pos, grid_for(m), kThreads, 0, keys2, m, posv);
     unsigned long long cnt[4] = {0, 0, 0, 0};
     PGD_CUDA(ctx, cudaMemcpyAsync(cnt, ctr, sizeof(cnt), cudaMemcpyDeviceToHost, s));
     PGD_CUDA(ctx, cudaStreamSynchronize(s));
@@ -1163,12 +1236,14 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, uint32_t *tslot
         nitems = ni;
         if ((st = pgd_tmp_alloc(ctx, (void **)&items, (nitems + 1) * sizeof(int64_t)))) return st;
         PGD_LAUNCH(ctx, k_item_fill, grid_for(nh), kThreads, 0, flag, fpos, (int64_t)nh, items);
+        if ((st = pgd_tmp_alloc(ctx, (void **)&hrec, (nh + 1) * sizeof(int2)))) return st;
+        PGD_LAUNCH(ctx, k_hub_recs, grid_for(nh), kThreads, 0, G, posv, (int64_t)nh, hrec);
     }
     const int nsm = ctx->num_sms;
     if (nitems > 0) {
         HubArgs H;
         const size_t smem = hub_layout(G.n, nhubs, max_degree, &H);
-        if (!H.smem_bitmap) {
+        if ((int64_t)H.split < G.n) {
             if ((st = pgd_tmp_alloc(ctx, (void **)&gbm, (size_t)nsm * H.nwords * 4))) return st;
             PGD_CUDA(ctx, cudaMemsetAsync(gbm, 0, (size_t)nsm * H.nwords * 4, s));
         }
@@ -1178,6 +1253,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, uint32_t *tslot
         PGD_CUDA(ctx, cudaFuncSetAttribute(k_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         H.G = G;
         H.hpos = posv;
+        H.hrec = hrec;
         H.items = items;
         H.nitems = nitems;
         H.ghist = ghist;
@@ -1209,11 +1285,13 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, uint32_t *tslot
     pgd_tmp_free(ctx, keys);
     pgd_tmp_free(ctx, keys2);
     pgd_tmp_free(ctx, posv);
+    pgd_tmp_free(ctx, vals);
     pgd_tmp_free(ctx, flag);
     pgd_tmp_free(ctx, fpos);
     pgd_tmp_free(ctx, items);
     pgd_tmp_free(ctx, ghist);
     pgd_tmp_free(ctx, gbm);
+    pgd_tmp_free(ctx, hrec);
     PGD_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
     PGD_CUDA(ctx, cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
     return PGD_OK;
@@ -1229,7 +1307,7 @@ pgd_status pgd_dev_decompose(pgd_graph *g, bool micro, pgd_counts *out) {
     if ((!g->has_aux || g->aux_cache_hub != ctx->cache_hub) && (st = build_aux(g))) return st;
     PGD_CUDA(ctx, cudaMemsetAsync(ctx->d_sums, 0, PGD_NSUMS * sizeof(unsigned long long), s));
     float ms = 0;
-    if ((st = run_decompose(ctx, dev_view(g, micro), g->tslot, g->nhubs, g->max_degree, &ms))) return st;
+    if ((st = run_decompose(ctx, dev_view(g, micro), (int4 *)g->slot, g->nhubs, g->max_degree, &ms))) return st;
     unsigned long long h[PGD_NSUMS];
     PGD_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_sums, sizeof(h), cudaMemcpyDeviceToHost, s));
     PGD_CUDA(ctx, cudaStreamSynchronize(s));
@@ -1384,11 +1462,12 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
         pgd_graph_free(&U, U.hubid, (N + 1) * sizeof(int32_t));
         pgd_graph_free(&U, U.vrank, (N + 1) * sizeof(int32_t));
         pgd_graph_free(&U, U.adjp_rank, (M + 1) * sizeof(int32_t));
-        pgd_graph_free(&U, U.tslot, (S + 1) * sizeof(uint32_t));
+        pgd_graph_free(&U, U.slot, (S + 1) * sizeof(int4));
         pgd_graph_free(&U, U.offh, (N + 1) * sizeof(int64_t));
         pgd_graph_free(&U, U.adjh, (U.nadjh + 1) * sizeof(int32_t));
         pgd_graph_free(&U, U.toprows, (U.top_words + 1) * sizeof(uint32_t));
         pgd_graph_free(&U, U.vrec, (N + 1) * 32);
+        pgd_graph_free(&U, U.adj_rank, (S + 1) * sizeof(int32_t));
     };
 #define BATCH_TRY(expr)                      \
     do {                                     \
@@ -1440,7 +1519,7 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
     G.gdense = ndense_graphs ? d_gdense : nullptr;
     DenseView dv{(const uint64_t *)bits, d_wbase, d_bases};
     float ms = 0;
-    BATCH_TRY(run_decompose(ctx, G, U.tslot, U.nhubs, U.max_degree, &ms, ndense_graphs ? &dv : nullptr));
+    BATCH_TRY(run_decompose(ctx, G, (int4 *)U.slot, U.nhubs, U.max_degree, &ms, ndense_graphs ? &dv : nullptr));
     std::vector<unsigned long long> h((size_t)k * PGD_NSUMS);
     if (cudaMemcpyAsync(h.data(), gsums, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s)) {
         cleanup();
@@ -1596,14 +1675,16 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     NA_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
     const int64_t m = nnz / 2;
     const int64_t nwords = (n + 31) / 32;
-    const bool in_smem = nwords * 4 <= kMaxSmemBitmap;
     const int64_t hub_bound = std::max<int64_t>(1, std::min<int64_t>(n, nnz / kCacheHub + 1));
 
     // CUB temporary storage sizes (queries only)
-    size_t tb_scan = 0, tb_sort = 0;
+    size_t tb_scan = 0, tb_sort = 0, tb_pairs = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, tb_scan, (uint32_t *)nullptr, (uint32_t *)nullptr, std::max(nnz, n) + 1, s);
     cub::DeviceRadixSort::SortKeys(nullptr, tb_sort, (uint64_t *)nullptr, (uint64_t *)nullptr,
                                    std::max<int64_t>(std::max(m, n), 1), 0, 64, s);
+    cub::DeviceRadixSort::SortPairs(nullptr, tb_pairs, (uint64_t *)nullptr, (uint64_t *)nullptr, (int32_t *)nullptr,
+                                    (int32_t *)nullptr, std::max<int64_t>(m, 1), 0, 64, s);
+    tb_sort = std::max(tb_sort, tb_pairs);
 
     // carve every buffer up front, with upper bounds, so an oversized graph
     // is refused before anything runs
@@ -1624,21 +1705,29 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     int32_t *adjp_rank = C.take<int32_t>(m + 1);
     uint64_t *rk = C.take<uint64_t>(n + 1);
     uint64_t *rk2 = C.take<uint64_t>(n + 1);
-    uint32_t *tslot = C.take<uint32_t>(nnz + 1);
+    int4 *slot = C.take<int4>(nnz + 1);
     uint64_t *keys = C.take<uint64_t>(m + 1);
     uint64_t *keys2 = C.take<uint64_t>(m + 1);
     int32_t *posv = C.take<int32_t>(m + 1);
+    int32_t *vals = C.take<int32_t>(m + 1);
     uint32_t *iflag = C.take<uint32_t>(m + 2);
     uint32_t *ipos = C.take<uint32_t>(m + 2);
     int64_t *items = C.take<int64_t>(m + 2);
+    int2 *hrec = C.take<int2>(m + 1);
     int64_t *offh = C.take<int64_t>(n + 1);
     int4 *vrec = C.take<int4>(2 * (n + 1));
     int32_t *adjh = C.take<int32_t>(nnz + 1);
+    // k_hub's layout depends on the hub count, known only later: carve for
+    // the largest possible count (the maximum degree is not known here
+    // either: 32-bit counters)
     HubArgs H;
-    // the maximum degree is not known here: 32-bit counters
     hub_layout(n, (int32_t)hub_bound, 1 << 30, &H);
+    // fewer hubs never need more global memory: a histogram that fits in
+    // shared memory for hub_bound hubs fits for fewer, and the bitmap's
+    // shared part only grows
     uint32_t *ghist = H.smem_hist ? nullptr : C.take<uint32_t>((size_t)nsm * H.hstride);
-    uint32_t *gbm = in_smem ? nullptr : C.take<uint32_t>((size_t)nsm * nwords);
+    uint32_t *gbm = (int64_t)H.split >= n ? nullptr : C.take<uint32_t>((size_t)nsm * nwords);
+    int32_t *adj_rank = C.take<int32_t>(nnz + 1);
     void *tmp = C.take<unsigned char>(std::max(tb_scan, tb_sort) + 16);
     if (!C.ok) {
         na_msg(err, errlen, "graph too large for the allocation-free path: needs more than the " +
@@ -1691,7 +1780,9 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     NA_CUDA(cub::DeviceRadixSort::SortKeys(tmp, tb, rk, rk2, n, 0, 64, s));
     k_rank_scatter<<<grid_for(n), kThreads, 0, s>>>(rk2, n, vrank);
     k_gather_rank<<<grid_for(m), kThreads, 0, s>>>(adjp, vrank, m, adjp_rank);
+    k_gather_rank<<<grid_for(nnz), kThreads, 0, s>>>(d_adj, vrank, nnz, adj_rank);
     k_vrec<<<grid_for(n), kThreads, 0, s>>>(d_off, offp, deg, vrank, hubid, n, vrec);
+    k_slot_fill<<<grid_for(nnz), kThreads, 0, s>>>(d_adj, vrank, hubid, offp, nnz, 0, slot);
 
     DevGraph G;
     G.off = d_off;
@@ -1700,7 +1791,7 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     G.offp = offp;
     G.adjp = adjp;
     G.hubid = hubid;
-    G.tslot = tslot;
+    G.slot = slot;
     G.ev = ev;
     G.eu = eu;
     G.order = order;
@@ -1713,16 +1804,16 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     G.gdense = nullptr;
     G.vrank = vrank;
     G.adjp_rank = adjp_rank;
+    G.adj_rank = adj_rank;
     G.offh = offh;
     G.adjh = adjh;
     G.toprows = nullptr;   // no rank-bitmap rows here: k4 always scans N+(x)
     G.vrec = vrec;
     G.top_r = 0;
     G.anchor_hub = kAnchorHub;
-    k_tslot<<<grid_for(32 * m), kThreads, 0, s>>>(G, tslot);
-    k_plan_keys<<<grid_for(m), kThreads, 0, s>>>(G, keys, ctr);
-    NA_CUDA(cub::DeviceRadixSort::SortKeys(tmp, tb, keys, keys2, m, 0, 64, s));
-    k_keys_pos<<<grid_for(m), kThreads, 0, s>>>(keys2, m, posv);
+    k_tslot<<<grid_for(32 * m), kThreads, 0, s>>>(G, slot);
+    k_plan_keys<<<grid_for(m), kThreads, 0, s>>>(G, keys, vals, ctr);
+    NA_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tb, keys, keys2, vals, posv, m, 0, 64, s));
     unsigned long long nh = 0;
     NA_CUDA(cudaMemcpyAsync(&nh, ctr, sizeof(nh), cudaMemcpyDeviceToHost, s));
     NA_CUDA(cudaStreamSynchronize(s));
@@ -1736,19 +1827,20 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
         NA_CUDA(cudaStreamSynchronize(s));
         nitems = ni;
         k_item_fill<<<grid_for(nh), kThreads, 0, s>>>(iflag, ipos, (int64_t)nh, items);
+        k_hub_recs<<<grid_for(nh), kThreads, 0, s>>>(G, posv, (int64_t)nh, hrec);
     }
     if (nitems > 0) {
-        // the layout carved above was sized for hub_bound hubs; the
-        // histogram only needs the actual count
+        // the layout for the actual hub count (the carve above covers it)
         const size_t smem = hub_layout(n, (int32_t)nhubs, 1 << 30, &H);
-        if (!H.smem_hist && !ghist) {
-            na_msg(err, errlen, "internal: histogram layout changed");
+        if ((!H.smem_hist && !ghist) || ((int64_t)H.split < n && !gbm)) {
+            na_msg(err, errlen, "internal: k_hub layout needs a global slice that was not carved");
             return PGD_ECUDA;
         }
-        if (!in_smem) NA_CUDA(cudaMemsetAsync(gbm, 0, (size_t)nsm * nwords * 4, s));
+        if ((int64_t)H.split < n) NA_CUDA(cudaMemsetAsync(gbm, 0, (size_t)nsm * nwords * 4, s));
         NA_CUDA(cudaFuncSetAttribute(k_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         H.G = G;
         H.hpos = posv;
+        H.hrec = hrec;
         H.items = items;
         H.nitems = nitems;
         H.ghist = ghist;
@@ -1969,7 +2061,7 @@ pgd_status pgd_dev_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pai
         G.gnm = d_gnm;
         G.gdense = ndense_graphs ? d_gdense : nullptr;
         DenseView dv{(const uint64_t *)bits, d_wbase, d_vbase};
-        PB_TRY(run_decompose(ctx, G, U->tslot, U->nhubs, U->max_degree, &ms, ndense_graphs ? &dv : nullptr));
+        PB_TRY(run_decompose(ctx, G, (int4 *)U->slot, U->nhubs, U->max_degree, &ms, ndense_graphs ? &dv : nullptr));
     }
     std::vector<unsigned long long> h((size_t)k * PGD_NSUMS);
     PB_CUDA(cudaMemcpyAsync(h.data(), gsums, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));

@@ -69,12 +69,13 @@ struct pgd_graph {
     int32_t *adjh = nullptr;          // nadjh: hub ids of each vertex's hub neighbours
     int64_t nadjh = 0;
     uint32_t *toprows = nullptr;      // rank-bitmap rows of N+(x) for the top_r highest-ranked x
+    int32_t *adj_rank = nullptr;      // 2m: vrank of each adjacency entry
     void *vrec = nullptr;             // n * 32 B: per-vertex record for the scans (decompose.cu)
     int32_t top_r = 0;
     int64_t top_words = 0;
     int32_t *vrank = nullptr;         // n: rank by (degree desc, id)
     int32_t *adjp_rank = nullptr;     // m: vrank of each adjp entry
-    uint32_t *tslot = nullptr;        // 2m: triangle count of each slot's edge
+    void *slot = nullptr;             // 2m * 16 B: per adjacency slot {w, vrank(w) | row flag, hubid(w), t}
 };
 
 // Launch one of this library's kernels on the context's stream and count it.

@@ -37,9 +37,12 @@ __device__ __forceinline__ int pgd_warp_incl_scan(int x) {
     return x;
 }
 
-// (unsigned long long)(x / 2.0) as the reference computes it: exact
-// conversion to double (round to nearest), scale, truncate.
+// (unsigned long long)(x / 2.0) as the reference computes it: conversion to
+// double (round to nearest), scale, truncate.  Below 2^53 the conversion and
+// the halving are exact, so the result is x >> 1; only larger x take the
+// double path (FP64 is slow on this part, and every edge needs several).
 __device__ __forceinline__ unsigned long long pgd_half_d(unsigned long long x) {
+    if ((x >> 53) == 0) return x >> 1;
     return __double2ull_rz(__dmul_rn(__ull2double_rn(x), 0.5));
 }
 
@@ -79,12 +82,25 @@ __device__ __forceinline__ unsigned long long pgd_micro_col(int c, long long dv,
     case 0: return t;
     case 1: return ((ull)dv - t) + ((ull)du - t) - 2;
     case 2: return k4;
-    case 3: return __double2ull_rz(__dsub_rn(__dmul_rn(__ull2double_rn(t * (t - 1)), 0.5), __ull2double_rn(k4)));
+    case 3: {
+        // (ull)((double)(t(t-1)) * 0.5 - (double)k4): exact below 2^53
+        const ull tt = t * (t - 1);
+        if ((tt >> 53) == 0 && (k4 >> 53) == 0) return (tt >> 1) - k4;
+        return __double2ull_rz(__dsub_rn(__dmul_rn(__ull2double_rn(tt), 0.5), __ull2double_rn(k4)));
+    }
     case 4: return 0;  // local_4_tailed_tris is never written (graphlet_core.cpp:1501)
     case 5: return c4;
     case 6: {
-        ull a = __double2ull_rz(__dmul_rn(__ll2double_rn(sv * (sv - 1)), 0.5));
-        return __double2ull_rz(__dadd_rn(__ull2double_rn(a), __dmul_rn(__ll2double_rn(su * (su - 1)), 0.5)));
+        // (ull)((double)a + (double)(su(su-1)) * 0.5), a = (ull)((double)(sv(sv-1)) * 0.5):
+        // exact while every operand and the sum stay below 2^53
+        const long long pv = sv * (sv - 1), pu = su * (su - 1);
+        const long long lim = 1ll << 53;
+        if (pv >= 0 && pv < lim && pu >= 0 && pu < lim) {
+            const ull a = (ull)pv >> 1, b = (ull)pu >> 1;
+            if (((a + b) >> 53) == 0) return a + b;
+        }
+        ull a = __double2ull_rz(__dmul_rn(__ll2double_rn(pv), 0.5));
+        return __double2ull_rz(__dadd_rn(__ull2double_rn(a), __dmul_rn(__ll2double_rn(pu), 0.5)));
     }
     default: return (ull)(sv * su) - c4;
     }

@@ -88,14 +88,16 @@ def test_autotune_keeps_counts():
     c.close()
 
 
-@pytest.mark.parametrize("case", ["hist16_global", "hist32_global", "bitmap_global"])
+@pytest.mark.parametrize("case", ["hist16_global", "hist32_global", "bitmap_split", "bitmap_large_n"])
 def test_hub_kernel_layouts(case):
-    """k_hub keeps the N(p) bitmap and the W histogram (16-bit counters when
-    the maximum degree is below 65536, else 32-bit) in shared memory when
-    they fit, else in per-CTA global slices; every combination gives the
-    oracle's counts."""
+    """k_hub keeps the W histogram (16-bit counters when the maximum degree is
+    below 65536, else 32-bit) in shared memory when it fits, and the N(p)
+    bitmap over degree ranks in the rest of shared memory, with per-CTA
+    global slices for what does not fit; every layout gives the oracle's
+    counts."""
     c = pgd.Context()
     n_min = 0
+    smem = 156 * 1024
     if case == "hist16_global":
         # 120k hubs (every vertex) at 2 B each do not fit in shared memory
         c.set_thresholds(2, 2)
@@ -107,19 +109,28 @@ def test_hub_kernel_layouts(case):
         leaves = np.arange(70000, dtype=np.int32)
         s = np.concatenate([s0, leaves])
         d = np.concatenate([d0, np.full(70000, 70000, np.int32)])
+    elif case == "bitmap_split":
+        # 78k hubs fill shared memory with counters: only the ~30k highest
+        # ranks of the bitmap stay shared, the rest are in global memory
+        c.set_thresholds(2, 2)
+        s, d = pgd.barabasi_albert(78000, 6, seed=14)
     else:
-        # 2M vertices (mostly isolated): the bitmap (n bits) goes to global memory
+        # 2M vertices (mostly isolated): the bitmap's tail is in global memory
         s, d = pgd.rmat(12, 16, seed=12)
         n_min = 2_000_000
     g = c.graph_from_edges(s, d, n_min=n_min)
     og = ol.OracleGraph.from_pairs(s, d, n_min=n_min, dedup=True)
     deg = np.diff(og.csr()[0])
+    n = len(deg)
     if case == "hist16_global":
-        assert deg.max() < 65536 and (deg >= 2).sum() * 2 + len(deg) / 8 > 188 * 1024
+        assert deg.max() < 65536 and (deg >= 2).sum() * 2 > smem
     elif case == "hist32_global":
-        assert deg.max() >= 65536 and (deg >= 2).sum() * 4 + len(deg) / 8 > 188 * 1024
+        assert deg.max() >= 65536 and (deg >= 2).sum() * 4 > smem
+    elif case == "bitmap_split":
+        hist = ((deg >= 2).sum() + 1) // 2 * 4
+        assert deg.max() < 65536 and hist <= smem and (smem - hist) * 8 < n // 2
     else:
-        assert len(deg) / 8 > 160 * 1024
+        assert n / 8 > smem
     r = g.decompose(micro=True)
     o = og.run()
     assert (r.totals == o.totals()).all()
