@@ -4,6 +4,7 @@
     python -m pgd_gb300.benchmarks serve [--requests 2000] [--rate 4000 | --rates 1000,4000,...] [--seed 1]
     python -m pgd_gb300.benchmarks large [--workloads rmat24,rgg24] [--samples 1000]
     python -m pgd_gb300.benchmarks profile [--scale 18] [--order kcore] [--reps 1]
+    python -m pgd_gb300.benchmarks small [--reps 50]
 
 batch: 4096 independent graphs, n uniform in [16, 2048]; half G(n, p) with p
 uniform in [0.01, 0.5], half Barabasi-Albert with m uniform in {2..8}; all
@@ -27,6 +28,10 @@ per-edge counts.  Timed: sort_edges + decomposition of the resident graph
 separately.  Checked: the per-edge columns against the global sums, the
 closing identities, and a seeded random sample of rows plus the heaviest rows
 against the oracle's marking procedure on those edges.
+
+small: G(n=250, p=0.9), seed 1 (the small dense configuration), degree
+order, per-edge counts; decomposition timed over `reps` runs on the resident
+graph, and end to end (host pairs in, host rows out) likewise.  edges/s.
 
 profile: one RMAT graph of the given scale, k-core order, decomposed `reps`
 times with per-edge counts; prints the kernel time of each run.  This is the
@@ -220,6 +225,38 @@ def run_profile(args):
                           "m": int(res.m), "kernel_ms": float(res.kernel_ms)}), flush=True)
 
 
+def run_small(args):
+    s, d = pgd.erdos_renyi(250, 0.9, seed=1)
+    ctx = pgd.Context()
+    g = ctx.graph_from_edges(s, d)
+    g.preprocess("deg")
+    g.sort_edges("deg")
+    for _ in range(5):
+        g.decompose(micro=True)
+    t0 = time.perf_counter()
+    kern = []
+    for _ in range(args.reps):
+        r = g.decompose(micro=True)
+        kern.append(r.kernel_ms)
+    dt = (time.perf_counter() - t0) / args.reps
+    m = int(r.m)
+    cols = np.empty((m, pgd.NMICRO), np.uint64)
+    s1 = np.empty(m, np.int64)
+    d1 = np.empty(m, np.int64)
+    t0 = time.perf_counter()
+    for _ in range(args.reps):
+        ge = ctx.graph_from_edges(s, d)
+        ge.preprocess("deg")
+        ge.sort_edges("deg")
+        ge.decompose(micro=True)
+        pgd.lib().pgd_get_micro(ge.h, pgd._ptr(s1), pgd._ptr(d1), pgd._ptr(cols))
+        ge.destroy()
+    e2e = (time.perf_counter() - t0) / args.reps
+    print(json.dumps({"mode": "small", "graph": "G(250, 0.9) seed 1", "n": int(r.n), "m": m,
+                      "decompose_ms": dt * 1000, "kernel_ms": float(np.median(kern)), "edges_per_s": m / dt,
+                      "e2e_ms": e2e * 1000, "e2e_edges_per_s": m / e2e}), flush=True)
+
+
 def large_pairs(name, seed):
     if name == "rmat24":
         return pgd.rmat(24, 16, seed=seed, **RMAT), "RMAT scale 24, edge factor 16, (0.57,0.19,0.19,0.05)"
@@ -287,7 +324,7 @@ def run_large(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("mode", choices=["batch", "serve", "large", "profile"])
+    ap.add_argument("mode", choices=["batch", "serve", "large", "profile", "small"])
     ap.add_argument("--workloads", default="rmat24,rgg24")
     ap.add_argument("--samples", type=int, default=1000)
     ap.add_argument("--heavy", type=int, default=10)
@@ -308,6 +345,8 @@ def main():
         run_serve(args)
     elif args.mode == "large":
         run_large(args)
+    elif args.mode == "small":
+        run_small(args)
     else:
         run_profile(args)
 

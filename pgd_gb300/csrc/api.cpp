@@ -373,17 +373,20 @@ extern "C" pgd_status pgd_get_micro(pgd_graph *g, int64_t *src1, int64_t *dst1, 
     cudaSetDevice(g->ctx->device);
     if (cols && g->m)
         PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, cols, g->micro, g->m * PGD_NMICRO * sizeof(uint64_t), cudaMemcpyDeviceToHost));
-    if (src1 || dst1) {
-        std::vector<int32_t> ev((size_t)g->m + 1), eu((size_t)g->m + 1), ord((size_t)g->m + 1);
-        if (g->m) {
-            PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, ev.data(), g->ev, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
-            PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, eu.data(), g->eu, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
-            PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, ord.data(), g->order, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
-        }
-        for (int64_t e = 0; e < g->m; e++) {
-            if (src1) src1[e] = (int64_t)ev[ord[e]] + 1;
-            if (dst1) dst1[e] = (int64_t)eu[ord[e]] + 1;
-        }
+    if ((src1 || dst1) && g->m) {
+        // ids gathered on the device, then copied straight into the caller's arrays
+        int64_t *d_ids = nullptr;
+        pgd_status st = pgd_tmp_alloc(g->ctx, (void **)&d_ids, 2 * g->m * sizeof(int64_t));
+        if (st) return st;
+        st = pgd_dev_micro_ids(g, src1 ? d_ids : nullptr, dst1 ? d_ids + g->m : nullptr);
+        cudaError_t e = cudaSuccess;
+        if (!st && src1)
+            e = pgd_copy_sync(g->ctx, src1, d_ids, g->m * sizeof(int64_t), cudaMemcpyDeviceToHost);
+        if (!st && e == cudaSuccess && dst1)
+            e = pgd_copy_sync(g->ctx, dst1, d_ids + g->m, g->m * sizeof(int64_t), cudaMemcpyDeviceToHost);
+        pgd_tmp_free(g->ctx, d_ids);
+        if (st) return st;
+        if (e != cudaSuccess) return pgd_cuda_fail(g->ctx, e, "copy of the per-edge ids");
     }
     return PGD_OK;
 }

@@ -730,3 +730,23 @@ pgd_status pgd_dev_sort_edges(pgd_graph *g, int kind, int s2l) {
     g->sorted = true;
     return PGD_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Row ids of the per-edge output (the writer's id+1 convention,
+// graphlet_core.cpp:1694-1701): row e is edge order[e].
+
+__global__ void k_micro_ids(const int32_t *ev, const int32_t *eu, const int32_t *order, int64_t m, int64_t *src1,
+                            int64_t *dst1) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t id = order[e];
+        if (src1) src1[e] = (int64_t)ev[id] + 1;
+        if (dst1) dst1[e] = (int64_t)eu[id] + 1;
+    }
+}
+
+pgd_status pgd_dev_micro_ids(pgd_graph *g, int64_t *d_src1, int64_t *d_dst1) {
+    pgd_ctx *ctx = g->ctx;
+    if (g->m > 0) PGD_LAUNCH(ctx, k_micro_ids, grid_for(g->m), kThreads, 0, g->ev, g->eu, g->order, g->m, d_src1, d_dst1);
+    PGD_CUDA(ctx, cudaGetLastError());
+    return PGD_OK;
+}

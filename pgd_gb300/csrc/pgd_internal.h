@@ -113,6 +113,7 @@ pgd_status pgd_dev_preprocess(pgd_graph *g, int neigh_kind, int s2l);
 pgd_status pgd_dev_cores(pgd_graph *g);
 pgd_status pgd_dev_assortativity(pgd_graph *g, double *r);
 pgd_status pgd_dev_sort_edges(pgd_graph *g, int order_kind, int s2l);
+pgd_status pgd_dev_micro_ids(pgd_graph *g, int64_t *d_src1, int64_t *d_dst1);
 
 // Decomposition (decompose.cu).
 pgd_status pgd_dev_decompose(pgd_graph *g, bool micro, pgd_counts *out);
