@@ -62,6 +62,7 @@ constexpr int kChunk = 2048;             // edges of one anchor per CTA work ite
 constexpr int kMaxChunks = 8;            // ... but an anchor is split into at most this many items, since
                                          // every item rebuilds the anchor's bitmap and W histogram
 constexpr int kMaxDynSmem = 156 * 1024;  // k_hub dynamic shared memory: bitmap, then the W histogram
+constexpr int kMaxTslotSmem = 200 * 1024;  // k_tslot_hub dynamic shared memory: rank bitmap
 constexpr int kRankBits = 16384;         // T members of degree rank below this are marked in a per-warp bitmap;
                                          // vertices of rank below this get a rank-bitmap row of N+(x)
 
@@ -227,12 +228,15 @@ __global__ void k_hub_ids(const uint32_t *flag, const uint32_t *pos, int64_t n, 
         hubid[v] = flag[v] ? (int32_t)pos[v] : -1;
 }
 
-// t of every edge, written to both of its CSR slots (the slot records' last field).  One warp per edge:
-// the shorter list's entries are searched in the longer one.
-__global__ void k_tslot(DevGraph G, int4 *slot) {
+// t of every edge (or of the edges at the E_ordered positions listed in pos),
+// written to both of its CSR slots (the slot records' last field).  One warp
+// per edge: the shorter list's entries are searched in the longer one.
+__global__ void k_tslot(DevGraph G, int4 *slot, const int32_t *pos, int64_t count) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t id = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; id < G.m; id += nw) {
+    const int64_t total = pos ? count : G.m;
+    for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < total; i += nw) {
+        const int64_t id = pos ? G.order[pos[i]] : i;
         // in a batch each graph's edge ids and E_ordered positions cover the
         // same range, so egraph[id] is the edge's graph
         if (dense_edge(G, id)) continue;
@@ -452,6 +456,7 @@ struct HubArgs {
     int64_t nwords;
     int32_t split;            // ranks below this are kept in shared memory
     unsigned long long *next;
+    int4 *slot_out;           // k_tslot_hub: slot records whose t it writes
 };
 
 // |{r in L[0..len) : r in N(p)}| for a list of ranks, warp-cooperative,
@@ -792,6 +797,72 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
         __syncthreads();
     }
     block_flush(G, acc, cur_g, s_red, kHubWarps);
+}
+
+// ---------------------------------------------------------------------------
+// t of the hub-anchored edges, grouped like k_hub's work items: per item the
+// anchor's neighbours go into the rank bitmap once, then each edge (p, q)
+// counts the entries of N(q) whose rank is set -- one coalesced pass over
+// q's ranks and shared-memory bit tests, instead of a binary search in N(p)
+// per entry.  Both CSR slots of the edge get t.
+
+__global__ void __launch_bounds__(kHubWarps * 32, 1) k_tslot_hub(HubArgs A) {
+    extern __shared__ __align__(16) uint32_t s_dyn[];
+    __shared__ long long s_item;
+    __shared__ int s_enext;
+    const DevGraph &G = A.G;
+    const int lane = threadIdx.x & 31;
+    RankBits bm;
+    bm.s = s_dyn;
+    bm.g = A.gbitmap ? A.gbitmap + (int64_t)blockIdx.x * A.nwords : nullptr;
+    bm.split = A.split;
+    for (int i = threadIdx.x; i < (A.split >> 5); i += blockDim.x) bm.s[i] = 0;
+    __syncthreads();
+    while (true) {
+        if (threadIdx.x == 0) {
+            s_item = (long long)atomicAdd(A.next, 1ull);
+            s_enext = 0;
+        }
+        __syncthreads();
+        const long long item = s_item;
+        if (item >= A.nitems) break;
+        const int64_t start = A.items[item], end = A.items[item + 1];
+        const int nedge = (int)(end - start);
+        int32_t p;
+        {
+            const int2 r0 = A.hrec[start];
+            const int32_t id = G.order[r0.x];
+            p = G.ev[id] == r0.y ? G.eu[id] : G.ev[id];
+        }
+        const int64_t offp = G.off[p];
+        const int dp = G.deg[p];
+        const int32_t *Rp = G.adj_rank + offp;
+        for (int i = threadIdx.x; i < dp; i += blockDim.x) bm.set(__ldg(Rp + i));
+        __syncthreads();
+        while (true) {
+            int k = 0;
+            if (lane == 0) k = atomicAdd(&s_enext, 1);
+            k = __shfl_sync(0xffffffffu, k, 0);
+            if (k >= nedge) break;
+            const int32_t q = __ldg(&A.hrec[start + k].y);
+            const int64_t offq = G.off[q];
+            const int dq = G.deg[q];
+            const int32_t *Rq = G.adj_rank + offq;
+            unsigned c = 0;
+            int i = lane;
+            for (; i + 96 < dq; i += 128) {
+                const int32_t r0 = __ldg(Rq + i), r1 = __ldg(Rq + i + 32), r2 = __ldg(Rq + i + 64), r3 = __ldg(Rq + i + 96);
+                c += bm.test(r0) + bm.test(r1) + bm.test(r2) + bm.test(r3);
+            }
+            for (; i < dq; i += 32) c += bm.test(__ldg(Rq + i));
+            c = __reduce_add_sync(0xffffffffu, c);
+            if (lane == 0) A.slot_out[offp + pgd_lower_bound(G.adj + offp, dp, q)].w = (int)c;
+            if (lane == 1) A.slot_out[offq + pgd_lower_bound(G.adj + offq, dq, p)].w = (int)c;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < dp; i += blockDim.x) bm.clear_word(__ldg(Rp + i));
+        __syncthreads();
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1206,7 +1277,6 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     unsigned long long *ctr = ctx->d_ctr;
     PGD_CUDA(ctx, cudaMemsetAsync(ctr, 0, 8 * sizeof(unsigned long long), s));
     PGD_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
-    PGD_LAUNCH(ctx, k_tslot, grid_for(32 * m), kThreads, 0, G, slot);
     PGD_LAUNCH(ctx, k_plan_keys, grid_for(m), kThreads, 0, G, keys, vals, ctr);
     size_t tb = 0;
     void *tmp = nullptr;
@@ -1240,13 +1310,32 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
         PGD_LAUNCH(ctx, k_hub_recs, grid_for(nh), kThreads, 0, G, posv, (int64_t)nh, hrec);
     }
     const int nsm = ctx->num_sms;
+    // triangle counts of every edge first: k_hub and k_light read t(x, q) of
+    // other edges.  Hub-anchored edges grouped by anchor, the rest one warp each
+    // (dense-graph edges need none).
+    HubArgs H;
+    const size_t smem = hub_layout(G.n, nhubs, max_degree, &H);
     if (nitems > 0) {
-        HubArgs H;
-        const size_t smem = hub_layout(G.n, nhubs, max_degree, &H);
         if ((int64_t)H.split < G.n) {
             if ((st = pgd_tmp_alloc(ctx, (void **)&gbm, (size_t)nsm * H.nwords * 4))) return st;
             PGD_CUDA(ctx, cudaMemsetAsync(gbm, 0, (size_t)nsm * H.nwords * 4, s));
         }
+        HubArgs T = H;
+        T.G = G;
+        T.hrec = hrec;
+        T.items = items;
+        T.nitems = nitems;
+        T.gbitmap = gbm;
+        T.next = ctr + 5;
+        T.slot_out = slot;
+        // the whole dynamic shared memory holds bitmap ranks (no histogram here)
+        const int64_t tw = std::min<int64_t>(H.nwords, kMaxTslotSmem / 4);
+        T.split = (int32_t)std::min<int64_t>(tw * 32, 0x7fffffe0);
+        PGD_CUDA(ctx, cudaFuncSetAttribute(k_tslot_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(tw * 4)));
+        PGD_LAUNCH(ctx, k_tslot_hub, nsm, kHubWarps * 32, (size_t)(tw * 4), T);
+    }
+    if (nlight > 0) PGD_LAUNCH(ctx, k_tslot, grid_for(32 * nlight), kThreads, 0, G, slot, posv + nh + nd, nlight);
+    if (nitems > 0) {
         if (!H.smem_hist) {
             if ((st = pgd_tmp_alloc(ctx, (void **)&ghist, (size_t)nsm * H.hstride * 4))) return st;
         }
@@ -1811,7 +1900,7 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     G.vrec = vrec;
     G.top_r = 0;
     G.anchor_hub = kAnchorHub;
-    k_tslot<<<grid_for(32 * m), kThreads, 0, s>>>(G, slot);
+    k_tslot<<<grid_for(32 * m), kThreads, 0, s>>>(G, slot, nullptr, 0);
     k_plan_keys<<<grid_for(m), kThreads, 0, s>>>(G, keys, vals, ctr);
     NA_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tb, keys, keys2, vals, posv, m, 0, 64, s));
     unsigned long long nh = 0;
