@@ -165,6 +165,21 @@ pgd_status pgd_assortativity(pgd_graph *g, double *r);
  * PGD_EUNSUPPORTED. */
 pgd_status pgd_sort_edges(pgd_graph *g, const char *order, int small_to_large);
 
+/* Edge order over a sample of edges.  Replaces the E_s overload of
+ * graphlet_core::sort_edges (graphlet_core.cpp:836-851): edge_ids[0..k) are
+ * edge ids (0 <= id < m, repeats allowed, k <= m) and the natural key is the
+ * position in the sample.  A following pgd_decompose decomposes only these
+ * k edges (sums and closed forms over the sample, with the whole graph's n
+ * and m; t of unsampled edges is still read), as the reference's
+ * decomposition iterates over E_ordered.  Batches reject sampled orders. */
+pgd_status pgd_sort_edges_sample(pgd_graph *g, const char *order, int small_to_large, const int64_t *edge_ids,
+                                 int64_t k);
+
+/* Length of E_ordered (m, or the sample size of pgd_sort_edges_sample; 0
+ * before any sort): the number of rows pgd_get_micro and the order array of
+ * pgd_get_edges hold.  No reference counterpart (E_ordered.size()). */
+int64_t pgd_graph_order_length(const pgd_graph *g);
+
 /* ---- decomposition ----------------------------------------------------- */
 
 #define PGD_MICRO 1u         /* also compute and keep the per-edge counts */
@@ -177,12 +192,14 @@ pgd_status pgd_decompose(pgd_graph *g, uint32_t flags, pgd_counts *out);
 
 /* Per-edge rows of the last PGD_MICRO decomposition in E_ordered order, as
  * write_micro_stats prints them (graphlet_core.cpp:1668-1761): src1/dst1 are
- * e_v+1 / e_u+1 (may be NULL), cols is m x 8 row-major: triangle, 2-star,
+ * e_v+1 / e_u+1 (may be NULL), cols is L x 8 row-major (L =
+ * pgd_graph_order_length, m unless the order is sampled): triangle, 2-star,
  * 4-clique, 4-chordal-cycle, 4-tailed-triangle, 4-cycle, 3-star, 4-path. */
 pgd_status pgd_get_micro(pgd_graph *g, int64_t *src1, int64_t *dst1, uint64_t *cols);
 
-/* Edge arrays e_v/e_u (graphlet_core.h:230) and E_ordered ids
- * (graphlet_core.h:206); any pointer may be NULL. */
+/* Edge arrays e_v/e_u (graphlet_core.h:230, m entries) and E_ordered ids
+ * (graphlet_core.h:206, pgd_graph_order_length entries); any pointer may be
+ * NULL. */
 pgd_status pgd_get_edges(pgd_graph *g, int64_t *ev, int64_t *eu, int32_t *order);
 
 /* Closing identities on the host (graphlet_core.cpp:1449-1472,

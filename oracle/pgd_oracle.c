@@ -532,7 +532,10 @@ static int cmp_incr(const void *a, const void *b) {
     return x->id > y->id ? -1 : (x->id < y->id);
 }
 
-int po_sort_edges(po_graph *g, const char *order, int s2l) {
+/* Both overloads of sort_edges: every edge (ids == NULL, the overload at
+ * graphlet_core.cpp:854-867) or the sample ids[0..k) (the E_s overload,
+ * :836-851, whose natural key is the position in the sample). */
+static int sort_edges_ids(po_graph *g, const char *order, int s2l, const int64_t *ids, int64_t k) {
     int kind;
     if (!strcmp(order, "natural")) kind = 0;
     else if (!strcmp(order, "deg") || !strcmp(order, "degree")) kind = 2;
@@ -558,10 +561,11 @@ int po_sort_edges(po_graph *g, const char *order, int s2l) {
         "common_neighbors", NULL};
     for (int i = 0; deg_u_names[i]; i++) if (!strcmp(order, deg_u_names[i])) kind = 99;
     if (kind == 3 || kind == 4 || kind == 6 || kind == 7) if (po_compute_cores(g)) return -1;
-    int64_t m = g->n_e;
+    int64_t m = ids ? k : g->n_e;
     ek_t *e = malloc((size_t)(m + 1) * sizeof(ek_t));
     for (int64_t i = 0; i < m; i++) {
-        int64_t v = g->ev[i], u = g->eu[i];
+        const int64_t eid = ids ? ids[i] : i;
+        int64_t v = g->ev[eid], u = g->eu[eid];
         long long val = i;
         switch (kind) {
         case 2: val = g->deg[u] + g->deg[v]; break;
@@ -584,7 +588,7 @@ int po_sort_edges(po_graph *g, const char *order, int s2l) {
         case 99: val = g->off[u + 1] - g->off[u]; break;
         default: break;
         }
-        e[i].id = (int32_t)i;
+        e[i].id = (int32_t)eid;
         e[i].key = (int32_t)val;
     }
     qsort(e, (size_t)m, sizeof(ek_t), s2l ? cmp_incr : cmp_decr);
@@ -594,6 +598,14 @@ int po_sort_edges(po_graph *g, const char *order, int s2l) {
     g->n_ord = m;
     free(e);
     return 0;
+}
+
+int po_sort_edges(po_graph *g, const char *order, int s2l) { return sort_edges_ids(g, order, s2l, NULL, 0); }
+
+int po_sort_edges_sample(po_graph *g, const char *order, int s2l, const int64_t *ids, int64_t k) {
+    for (int64_t i = 0; i < k; i++)
+        if (ids[i] < 0 || ids[i] >= g->n_e) return -1;
+    return sort_edges_ids(g, order, s2l, ids, k);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -890,6 +902,7 @@ int po_edge_sample(po_graph *g, int64_t k, const int64_t *vs, const int64_t *us,
 /* ------------------------------------------------------------------------ */
 int64_t po_n(const po_graph *g) { return g->n; }
 int64_t po_m(const po_graph *g) { return g->m; }
+int64_t po_n_ord(const po_graph *g) { return g->n_ord; }
 int po_max_degree(const po_graph *g) { return g->max_degree; }
 int po_max_core(const po_graph *g) { return g->max_core; }
 void po_get_csr(const po_graph *g, int64_t *off, int32_t *adj) {

@@ -49,6 +49,9 @@ int po_compute_cores(po_graph *g);
 double po_assortativity(po_graph *g);
 /* graphlet_core::sort_edges (graphlet_core.cpp:854-867). */
 int po_sort_edges(po_graph *g, const char *order, int s2l);
+/* sort_edges over a sample of edge ids (graphlet_core.cpp:836-851); the
+ * following po_decompose covers only those k positions. */
+int po_sort_edges_sample(po_graph *g, const char *order, int s2l, const int64_t *ids, int64_t k);
 /* graphlet_decomposition[_micro] (graphlet_core.cpp:1366-1625).  threads<=0
  * means all cores.  cheap_side!=0 scans the endpoint with the smaller 2-hop
  * volume instead of always e_u (same counts, less work on power-law graphs). */
@@ -73,6 +76,7 @@ void po_close(const uint64_t sums[PO_NSUMS], int64_t n, int64_t m, uint64_t tota
 /* Accessors. */
 int64_t po_n(const po_graph *g);
 int64_t po_m(const po_graph *g);
+int64_t po_n_ord(const po_graph *g);   /* E_ordered length: m or the sample size */
 int po_max_degree(const po_graph *g);
 int po_max_core(const po_graph *g);
 void po_get_csr(const po_graph *g, int64_t *off, int32_t *adj);

@@ -68,6 +68,19 @@ long long ref_run_sample(void *h, const char *order, int s2l, int workers, long 
     return (long long)sample.size();
 }
 
+// The reference's own sampled path: sort_edges with E_s = ids[0..k), then the
+// decomposition (per-edge rows too when micro).
+void ref_run_ids(void *h, const char *order, int s2l, const int64_t *ids, long long k, int micro, int workers) {
+    graphlet_core *g = (graphlet_core *)h;
+    g->compute_cores();
+    std::vector<unsigned long> sample((size_t)k);
+    for (long long i = 0; i < k; i++) sample[(size_t)i] = (unsigned long)ids[i];
+    g->E_ordered.clear();
+    g->sort_edges(std::string(order), s2l != 0, sample);
+    if (micro) g->graphlet_decomposition_micro(workers);
+    else g->graphlet_decomposition(workers);
+}
+
 void ref_totals(void *h, uint64_t *out) {
     graphlet_core *g = (graphlet_core *)h;
     const unsigned long long v[17] = {
@@ -86,6 +99,8 @@ int ref_is_adj(void *h) { return ((graphlet_core *)h)->is_adj_exists() ? 1 : 0; 
 
 // Rows in E_ordered order, as write_micro_stats prints them
 // (graphlet_core.cpp:1689-1701).
+int64_t ref_n_ord(void *h) { return (int64_t)((graphlet_core *)h)->E_ordered.size(); }
+
 void ref_micro(void *h, int64_t *src1, int64_t *dst1, uint64_t *cols) {
     graphlet_core *g = (graphlet_core *)h;
     for (long long e = 0; e < (long long)g->E_ordered.size(); e++) {

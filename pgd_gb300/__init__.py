@@ -47,7 +47,8 @@ EXPORTS = [
     "pgd_decompose_batch", "pgd_gen_u01", "pgd_gen_rmat", "pgd_gen_er", "pgd_gen_ba",
     "pgd_gen_rgg3d", "pgd_decompose_csr_noalloc", "pgd_noalloc_scratch_bytes", "pgd_set_thresholds",
     "pgd_get_thresholds", "pgd_autotune", "pgd_decompose_pairs_batch", "pgd_server_create", "pgd_server_submit",
-    "pgd_server_poll", "pgd_server_wait", "pgd_server_stats", "pgd_server_destroy",
+    "pgd_server_poll", "pgd_server_wait", "pgd_server_stats", "pgd_server_destroy", "pgd_sort_edges_sample",
+    "pgd_graph_order_length",
 ]
 
 
@@ -122,6 +123,8 @@ def lib():
             "pgd_get_kcore": (ctypes.c_int, [_P, _I32]),
             "pgd_assortativity": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),
             "pgd_sort_edges": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int]),
+            "pgd_sort_edges_sample": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int, _I64, ctypes.c_int64]),
+            "pgd_graph_order_length": (ctypes.c_int64, [_P]),
             "pgd_decompose": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.POINTER(pgd_counts)]),
             "pgd_get_micro": (ctypes.c_int, [_P, _P, _P, _P]),
             "pgd_get_edges": (ctypes.c_int, [_P, _P, _P, _P]),
@@ -346,6 +349,18 @@ class Graph:
         self.ctx._check(lib().pgd_sort_edges(self.h, order.encode(), int(s2l)), "pgd_sort_edges")
         return self
 
+    def sort_edges_sample(self, edge_ids, order="deg", s2l=False):
+        """Order (and later decompose) only the given edge ids (E_s)."""
+        ids = np.ascontiguousarray(edge_ids, dtype=np.int64)
+        self.ctx._check(lib().pgd_sort_edges_sample(self.h, order.encode(), int(s2l), ids, len(ids)),
+                        "pgd_sort_edges_sample")
+        return self
+
+    @property
+    def order_length(self):
+        """Length of E_ordered: m, or the sample size."""
+        return int(lib().pgd_graph_order_length(self.h))
+
     def decompose(self, micro=False):
         c = pgd_counts()
         self.ctx._check(lib().pgd_decompose(self.h, MICRO if micro else 0, ctypes.byref(c)),
@@ -353,7 +368,7 @@ class Graph:
         return Counts(c)
 
     def micro(self, ids=True, out=None):
-        m = self.m
+        m = self.order_length
         cols = out if out is not None else np.empty((max(m, 1), NMICRO), np.uint64)
         src = np.empty(max(m, 1), np.int64) if ids else None
         dst = np.empty(max(m, 1), np.int64) if ids else None
@@ -368,7 +383,7 @@ class Graph:
         eu = np.empty(max(m, 1), np.int64)
         order = np.empty(max(m, 1), np.int32) if with_order else None
         self.ctx._check(lib().pgd_get_edges(self.h, _ptr(ev), _ptr(eu), _ptr(order)), "pgd_get_edges")
-        return ev[:m], eu[:m], (order[:m] if with_order else None)
+        return ev[:m], eu[:m], (order[:self.order_length] if with_order else None)
 
 
 class Server:

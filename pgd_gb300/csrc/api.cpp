@@ -334,6 +334,25 @@ extern "C" pgd_status pgd_sort_edges(pgd_graph *g, const char *order, int small_
     return pgd_dev_sort_edges(g, kind, small_to_large);
 }
 
+extern "C" pgd_status pgd_sort_edges_sample(pgd_graph *g, const char *order, int small_to_large,
+                                            const int64_t *edge_ids, int64_t k) {
+    if (!g || k < 0 || (k > 0 && !edge_ids)) return g ? pgd_fail(g->ctx, PGD_EINVAL, "bad arguments") : PGD_EINVAL;
+    cudaSetDevice(g->ctx->device);
+    int kind = parse_order(order);
+    if (kind < 0)
+        return pgd_fail(g->ctx, PGD_EUNSUPPORTED,
+                        std::string("edge ordering '") + (order ? order : "") +
+                            "' is wall-clock seeded or divides by zero in the reference");
+    pgd_status st;
+    if (!g->preprocessed && (st = pgd_preprocess(g, "deg", 0))) return st;
+    bool need_cores = kind == PGD_ORD_KCORE || kind == PGD_ORD_KCORE_DEG || kind == PGD_ORD_KCORE_VOL ||
+                      kind == PGD_ORD_KCORE_DEG_VOL;
+    if (need_cores && !g->has_cores && (st = pgd_dev_cores(g))) return st;
+    return pgd_dev_sort_edges_sample(g, kind, small_to_large, edge_ids, k);
+}
+
+extern "C" int64_t pgd_graph_order_length(const pgd_graph *g) { return g && g->sorted ? g->norder : 0; }
+
 // ---------------------------------------------------------------------------
 // decomposition and results
 
@@ -362,7 +381,8 @@ extern "C" pgd_status pgd_get_edges(pgd_graph *g, int64_t *ev, int64_t *eu, int3
     }
     if (order) {
         if (!g->sorted) return pgd_fail(g->ctx, PGD_EINVAL, "edges are not sorted");
-        PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, order, g->order, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        if (g->norder)
+            PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, order, g->order, g->norder * sizeof(int32_t), cudaMemcpyDeviceToHost));
     }
     return PGD_OK;
 }
@@ -371,19 +391,20 @@ extern "C" pgd_status pgd_get_micro(pgd_graph *g, int64_t *src1, int64_t *dst1, 
     if (!g) return PGD_EINVAL;
     if (!g->has_micro) return pgd_fail(g->ctx, PGD_EINVAL, "no per-edge results: decompose with PGD_MICRO first");
     cudaSetDevice(g->ctx->device);
-    if (cols && g->m)
-        PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, cols, g->micro, g->m * PGD_NMICRO * sizeof(uint64_t), cudaMemcpyDeviceToHost));
-    if ((src1 || dst1) && g->m) {
+    if (cols && g->norder)
+        PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, cols, g->micro, g->norder * PGD_NMICRO * sizeof(uint64_t),
+                                       cudaMemcpyDeviceToHost));
+    if ((src1 || dst1) && g->norder) {
         // ids gathered on the device, then copied straight into the caller's arrays
         int64_t *d_ids = nullptr;
-        pgd_status st = pgd_tmp_alloc(g->ctx, (void **)&d_ids, 2 * g->m * sizeof(int64_t));
+        const int64_t k = g->norder;
+        pgd_status st = pgd_tmp_alloc(g->ctx, (void **)&d_ids, 2 * k * sizeof(int64_t));
         if (st) return st;
-        st = pgd_dev_micro_ids(g, src1 ? d_ids : nullptr, dst1 ? d_ids + g->m : nullptr);
+        st = pgd_dev_micro_ids(g, src1 ? d_ids : nullptr, dst1 ? d_ids + k : nullptr);
         cudaError_t e = cudaSuccess;
-        if (!st && src1)
-            e = pgd_copy_sync(g->ctx, src1, d_ids, g->m * sizeof(int64_t), cudaMemcpyDeviceToHost);
+        if (!st && src1) e = pgd_copy_sync(g->ctx, src1, d_ids, k * sizeof(int64_t), cudaMemcpyDeviceToHost);
         if (!st && e == cudaSuccess && dst1)
-            e = pgd_copy_sync(g->ctx, dst1, d_ids + g->m, g->m * sizeof(int64_t), cudaMemcpyDeviceToHost);
+            e = pgd_copy_sync(g->ctx, dst1, d_ids + k, k * sizeof(int64_t), cudaMemcpyDeviceToHost);
         pgd_tmp_free(g->ctx, d_ids);
         if (st) return st;
         if (e != cudaSuccess) return pgd_cuda_fail(g->ctx, e, "copy of the per-edge ids");

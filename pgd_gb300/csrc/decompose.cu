@@ -86,6 +86,7 @@ struct DevGraph {
     const int32_t *eu;
     const int32_t *order;
     long long n, m;
+    long long npos;             // E_ordered positions to decompose: m, or the sample size
     uint64_t *micro;
     unsigned long long *sums;   // PGD_NSUMS, or PGD_NSUMS per graph when batched
     const int32_t *egraph;      // batched: graph of each E_ordered position, else null
@@ -265,7 +266,7 @@ __global__ void k_tslot(DevGraph G, int4 *slot, const int32_t *pos, int64_t coun
 // 0xfffffffe, so the sorted order is [hub-anchored, by anchor][dense][light].
 __global__ void k_plan_keys(DevGraph G, uint64_t *keys, int32_t *vals, unsigned long long *counts) {
     unsigned long long hubs = 0, dense = 0;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < G.m; e += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < G.npos; e += (int64_t)gridDim.x * blockDim.x) {
         const int32_t id = G.order[e];
         const int32_t v = G.ev[id], u = G.eu[id];
         const int32_t p = ranks_above(v, u, G.deg) ? v : u;
@@ -1213,6 +1214,7 @@ static DevGraph dev_view(pgd_graph *g, bool micro) {
     G.order = g->order;
     G.n = g->n;
     G.m = g->m;
+    G.npos = g->norder;
     G.micro = micro ? g->micro : nullptr;
     G.sums = g->ctx->d_sums;
     G.egraph = nullptr;
@@ -1259,9 +1261,11 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
                                 float *ms, const DenseView *dense = nullptr) {
     cudaStream_t s = ctx->stream;
     pgd_status st;
-    const int64_t m = G.m;
+    const int64_t m = G.npos;   // positions to decompose (E_ordered length)
     *ms = 0;
     if (m == 0) return PGD_OK;
+    // a sampled order decomposes some edges but reads t(x, q) of any edge
+    const bool sampled = G.npos < G.m;
     uint64_t *keys = nullptr, *keys2 = nullptr;
     int32_t *posv = nullptr, *vals = nullptr;
     uint32_t *flag = nullptr, *fpos = nullptr;
@@ -1315,6 +1319,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     // (dense-graph edges need none).
     HubArgs H;
     const size_t smem = hub_layout(G.n, nhubs, max_degree, &H);
+    if (sampled) PGD_LAUNCH(ctx, k_tslot, grid_for(32 * G.m), kThreads, 0, G, slot, nullptr, 0);
     if (nitems > 0) {
         if ((int64_t)H.split < G.n) {
             if ((st = pgd_tmp_alloc(ctx, (void **)&gbm, (size_t)nsm * H.nwords * 4))) return st;
@@ -1331,10 +1336,13 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
         // the whole dynamic shared memory holds bitmap ranks (no histogram here)
         const int64_t tw = std::min<int64_t>(H.nwords, kMaxTslotSmem / 4);
         T.split = (int32_t)std::min<int64_t>(tw * 32, 0x7fffffe0);
-        PGD_CUDA(ctx, cudaFuncSetAttribute(k_tslot_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(tw * 4)));
-        PGD_LAUNCH(ctx, k_tslot_hub, nsm, kHubWarps * 32, (size_t)(tw * 4), T);
+        if (!sampled) {
+            PGD_CUDA(ctx, cudaFuncSetAttribute(k_tslot_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(tw * 4)));
+            PGD_LAUNCH(ctx, k_tslot_hub, nsm, kHubWarps * 32, (size_t)(tw * 4), T);
+        }
     }
-    if (nlight > 0) PGD_LAUNCH(ctx, k_tslot, grid_for(32 * nlight), kThreads, 0, G, slot, posv + nh + nd, nlight);
+    if (nlight > 0 && !sampled)
+        PGD_LAUNCH(ctx, k_tslot, grid_for(32 * nlight), kThreads, 0, G, slot, posv + nh + nd, nlight);
     if (nitems > 0) {
         if (!H.smem_hist) {
             if ((st = pgd_tmp_alloc(ctx, (void **)&ghist, (size_t)nsm * H.hstride * 4))) return st;
@@ -1472,6 +1480,9 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
     std::vector<long long> gnm((size_t)2 * k);
     int64_t N = 0, M = 0, S = 0;
     int32_t max_degree = 0;
+    for (int i = 0; i < k; i++)
+        if (graphs[i]->norder != graphs[i]->m)
+            return pgd_fail(ctx, PGD_EINVAL, "a graph of the batch has a sampled edge order (decompose it alone)");
     for (int i = 0; i < k; i++) {
         pgd_graph *g = graphs[i];
         if (micro && !g->micro) {
@@ -1506,6 +1517,7 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
     U.ctx = ctx;
     U.n = N;
     U.m = M;
+    U.norder = M;
     U.max_degree = max_degree;
     BatchDesc *d_desc = nullptr;
     int64_t *d_bases = nullptr;
@@ -1886,6 +1898,7 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     G.order = order;
     G.n = n;
     G.m = m;
+    G.npos = m;
     G.micro = nullptr;
     G.sums = sums;
     G.egraph = nullptr;
@@ -2090,6 +2103,7 @@ pgd_status pgd_dev_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pai
     PB_TRY(pgd_graph_alloc(U, (void **)&U->ev, (M + 1) * sizeof(int32_t)));
     PB_TRY(pgd_graph_alloc(U, (void **)&U->eu, (M + 1) * sizeof(int32_t)));
     PB_TRY(pgd_graph_alloc(U, (void **)&U->order, (M + 1) * sizeof(int32_t)));
+    U->norder = M;
     PB_TRY(pgd_tmp_alloc(ctx, (void **)&row, (nnz + 1) * sizeof(int32_t)));
     PB_TRY(pgd_tmp_alloc(ctx, (void **)&flag, (nnz + 1) * sizeof(uint32_t)));
     PB_TRY(pgd_tmp_alloc(ctx, (void **)&pos, (nnz + 1) * sizeof(uint32_t)));

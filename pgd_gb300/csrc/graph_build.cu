@@ -14,6 +14,7 @@
 // decides edge ids and hence the E_ordered tie-break; it is reproduced as a
 // per-entry "insertion rank" and a segmented sort, never materialised.
 #include <cub/cub.cuh>
+#include <vector>
 
 #include "pgd_internal.h"
 
@@ -304,11 +305,16 @@ __global__ void k_assort_partial(const int32_t *ev, const int32_t *eu, const int
 // int (Vertex, graphlet_vertex.h:42); order is key then id, id always
 // descending (decr_bound / incr_bound, graphlet_vertex.h:57-75).
 
+// Keys of the edges to order: every edge (ids == null, count == m) or the
+// sampled edge ids ids[0..count) (sort_edges with E_s, graphlet_core.cpp:
+// 836-851), whose natural key is the position in the sample.
 __global__ void k_edge_keys(const int32_t *ev, const int32_t *eu, const int32_t *deg, const int32_t *core,
-                            const uint64_t *vsum, int64_t m, int kind, int s2l, uint64_t *keys) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
+                            const uint64_t *vsum, const int32_t *ids, int64_t count, int kind, int s2l,
+                            uint64_t *keys) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = ids ? ids[i] : i;
         int32_t v = ev[e], u = eu[e];
-        long long val = e;
+        long long val = i;
         // core[] exists only for the k-core keys
         const bool kc = kind == PGD_ORD_KCORE || kind == PGD_ORD_KCORE_DEG;
         int kv = (kc && v >= 1) ? core[v - 1] : 0, ku = (kc && u >= 1) ? core[u - 1] : 0;
@@ -324,7 +330,7 @@ __global__ void k_edge_keys(const int32_t *ev, const int32_t *eu, const int32_t 
         }
         uint32_t k32 = (uint32_t)(int32_t)val ^ 0x80000000u;
         uint32_t id = (uint32_t)e;
-        keys[e] = ((uint64_t)k32 << 32) | (s2l ? (0xffffffffu - id) : id);
+        keys[i] = ((uint64_t)k32 << 32) | (s2l ? (0xffffffffu - id) : id);
     }
 }
 
@@ -691,7 +697,9 @@ pgd_status pgd_dev_assortativity(pgd_graph *g, double *r) {
     return PGD_OK;
 }
 
-pgd_status pgd_dev_sort_edges(pgd_graph *g, int kind, int s2l) {
+// Orders every edge (d_ids == null, count == m) or the sample d_ids[0..count)
+// (device array of edge ids in [0, m)); E_ordered gets count entries.
+static pgd_status sort_edges_impl(pgd_graph *g, int kind, int s2l, const int32_t *d_ids, int64_t count) {
     pgd_ctx *ctx = g->ctx;
     cudaStream_t s = ctx->stream;
     pgd_status st;
@@ -701,7 +709,8 @@ pgd_status pgd_dev_sort_edges(pgd_graph *g, int kind, int s2l) {
     }
     g->sorted = false;
     g->has_micro = false;
-    if (m == 0) { g->sorted = true; return PGD_OK; }
+    g->norder = count;
+    if (count == 0) { g->sorted = true; return PGD_OK; }
     uint64_t *vsum = nullptr;
     if (kind == PGD_ORD_DEG_VOL) {
         vsum = g->vol2;
@@ -711,24 +720,48 @@ pgd_status pgd_dev_sort_edges(pgd_graph *g, int kind, int s2l) {
                                                               kind == PGD_ORD_KCORE_VOL ? 1 : 2, vsum);
     }
     uint64_t *keys = nullptr, *keys2 = nullptr;
-    if ((st = pgd_tmp_alloc(ctx, (void **)&keys, m * sizeof(uint64_t)))) return st;
-    if ((st = pgd_tmp_alloc(ctx, (void **)&keys2, m * sizeof(uint64_t)))) return st;
-    PGD_LAUNCH(ctx, k_edge_keys, grid_for(m), kThreads, 0, g->ev, g->eu, g->deg, g->core, vsum, m, kind, s2l, keys);
+    if ((st = pgd_tmp_alloc(ctx, (void **)&keys, count * sizeof(uint64_t)))) return st;
+    if ((st = pgd_tmp_alloc(ctx, (void **)&keys2, count * sizeof(uint64_t)))) return st;
+    PGD_LAUNCH(ctx, k_edge_keys, grid_for(count), kThreads, 0, g->ev, g->eu, g->deg, g->core, vsum, d_ids, count, kind,
+               s2l, keys);
     size_t tb = 0;
     void *tmp = nullptr;
-    if (s2l) cub::DeviceRadixSort::SortKeys(nullptr, tb, keys, keys2, m, 0, 64, s);
-    else cub::DeviceRadixSort::SortKeysDescending(nullptr, tb, keys, keys2, m, 0, 64, s);
+    if (s2l) cub::DeviceRadixSort::SortKeys(nullptr, tb, keys, keys2, count, 0, 64, s);
+    else cub::DeviceRadixSort::SortKeysDescending(nullptr, tb, keys, keys2, count, 0, 64, s);
     if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
-    if (s2l) cub::DeviceRadixSort::SortKeys(tmp, tb, keys, keys2, m, 0, 64, s);
-    else cub::DeviceRadixSort::SortKeysDescending(tmp, tb, keys, keys2, m, 0, 64, s);
+    if (s2l) cub::DeviceRadixSort::SortKeys(tmp, tb, keys, keys2, count, 0, 64, s);
+    else cub::DeviceRadixSort::SortKeysDescending(tmp, tb, keys, keys2, count, 0, 64, s);
     pgd_tmp_free(ctx, tmp);
-    PGD_LAUNCH(ctx, k_keys_to_ids, grid_for(m), kThreads, 0, keys2, m, s2l, g->order);
+    PGD_LAUNCH(ctx, k_keys_to_ids, grid_for(count), kThreads, 0, keys2, count, s2l, g->order);
     pgd_tmp_free(ctx, keys);
     pgd_tmp_free(ctx, keys2);
     if (vsum && vsum != g->vol2) pgd_tmp_free(ctx, vsum);
     PGD_CUDA(ctx, cudaGetLastError());
     g->sorted = true;
     return PGD_OK;
+}
+
+pgd_status pgd_dev_sort_edges(pgd_graph *g, int kind, int s2l) { return sort_edges_impl(g, kind, s2l, nullptr, g->m); }
+
+pgd_status pgd_dev_sort_edges_sample(pgd_graph *g, int kind, int s2l, const int64_t *h_ids, int64_t k) {
+    pgd_ctx *ctx = g->ctx;
+    pgd_status st;
+    if (k < 0 || k > g->m) return pgd_fail(ctx, PGD_EINVAL, "sample size must be between 0 and m");
+    for (int64_t i = 0; i < k; i++)
+        if (h_ids[i] < 0 || h_ids[i] >= g->m) return pgd_fail(ctx, PGD_EINVAL, "sampled edge id out of range");
+    std::vector<int32_t> ids32((size_t)k + 1);
+    for (int64_t i = 0; i < k; i++) ids32[(size_t)i] = (int32_t)h_ids[i];
+    int32_t *d_ids = nullptr;
+    if ((st = pgd_tmp_alloc(ctx, (void **)&d_ids, (k + 1) * sizeof(int32_t)))) return st;
+    cudaError_t e = cudaMemcpyAsync(d_ids, ids32.data(), k * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);   // ids32 is a host temporary
+    if (e != cudaSuccess) {
+        pgd_tmp_free(ctx, d_ids);
+        return pgd_cuda_fail(ctx, e, "copy of the sampled edge ids");
+    }
+    st = sort_edges_impl(g, kind, s2l, d_ids, k);
+    pgd_tmp_free(ctx, d_ids);
+    return st;
 }
 
 // ---------------------------------------------------------------------------
@@ -746,7 +779,8 @@ __global__ void k_micro_ids(const int32_t *ev, const int32_t *eu, const int32_t 
 
 pgd_status pgd_dev_micro_ids(pgd_graph *g, int64_t *d_src1, int64_t *d_dst1) {
     pgd_ctx *ctx = g->ctx;
-    if (g->m > 0) PGD_LAUNCH(ctx, k_micro_ids, grid_for(g->m), kThreads, 0, g->ev, g->eu, g->order, g->m, d_src1, d_dst1);
+    if (g->norder > 0)
+        PGD_LAUNCH(ctx, k_micro_ids, grid_for(g->norder), kThreads, 0, g->ev, g->eu, g->order, g->norder, d_src1, d_dst1);
     PGD_CUDA(ctx, cudaGetLastError());
     return PGD_OK;
 }

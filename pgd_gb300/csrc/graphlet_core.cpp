@@ -140,7 +140,16 @@ void graphlet_core::compute_assortativity() {
 
 void graphlet_core::sort_edges(std::string edge_ordering, bool is_small_to_large) {
     check(pgd_sort_edges(graph_, edge_ordering.c_str(), is_small_to_large ? 1 : 0), "sort_edges");
-    E_ordered.assign((size_t)m_, 0);
+    E_ordered.assign((size_t)pgd_graph_order_length(graph_), 0);
+    check(pgd_get_edges(graph_, nullptr, nullptr, E_ordered.data()), "sort_edges");
+}
+
+void graphlet_core::sort_edges(std::string edge_ordering, bool is_small_to_large, std::vector<unsigned long> &E_s) {
+    std::vector<int64_t> ids(E_s.begin(), E_s.end());
+    check(pgd_sort_edges_sample(graph_, edge_ordering.c_str(), is_small_to_large ? 1 : 0, ids.data(),
+                                (int64_t)ids.size()),
+          "sort_edges");
+    E_ordered.assign((size_t)pgd_graph_order_length(graph_), 0);
     check(pgd_get_edges(graph_, nullptr, nullptr, E_ordered.data()), "sort_edges");
 }
 
@@ -157,14 +166,15 @@ void graphlet_core::decompose(bool micro) {
                                           &total_4_indep};
     for (int i = 0; i < PGD_NTOTALS; i++) *f[i] = c.totals[i];
     if (micro) {
-        std::vector<uint64_t> cols((size_t)m_ * PGD_NMICRO + 1);
+        const int64_t rows = pgd_graph_order_length(graph_);
+        std::vector<uint64_t> cols((size_t)rows * PGD_NMICRO + 1);
         check(pgd_get_micro(graph_, nullptr, nullptr, cols.data()), "micro counts");
         std::vector<unsigned long long> *dst[PGD_NMICRO] = {&tri, &two_star_, &local_4_clique,
                                                             &local_4_chordal_cycle, &local_4_tailed_tris,
                                                             &local_4_cycle, &local_3_star, &local_4_path};
         for (int c2 = 0; c2 < PGD_NMICRO; c2++) {
-            dst[c2]->resize((size_t)m_);
-            for (int64_t e = 0; e < m_; e++) (*dst[c2])[e] = cols[(size_t)e * PGD_NMICRO + c2];
+            dst[c2]->resize((size_t)rows);
+            for (int64_t e = 0; e < rows; e++) (*dst[c2])[e] = cols[(size_t)e * PGD_NMICRO + c2];
         }
     }
 }

@@ -35,6 +35,8 @@ class graphlet_core {
     void compute_cores();
     void compute_assortativity();
     void sort_edges(std::string edge_ordering = "degree", bool is_small_to_large = false);
+    // the E_s overload (graphlet_core.h:208-209): order and decompose only the sampled edge ids
+    void sort_edges(std::string edge_ordering, bool is_small_to_large, std::vector<unsigned long> &E_s);
     void graphlet_decomposition(int max_num_workers = 1);
     void graphlet_decomposition_micro(int max_num_workers = 1);
 

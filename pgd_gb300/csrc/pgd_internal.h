@@ -52,7 +52,8 @@ struct pgd_graph {
 
     // E_ordered edge ids
     bool sorted = false;
-    int32_t *order = nullptr;         // m
+    int32_t *order = nullptr;         // m entries allocated
+    int64_t norder = 0;               // E_ordered length: m, or the sample size
 
     // per-edge results in E_ordered order
     bool has_micro = false;
@@ -113,6 +114,7 @@ pgd_status pgd_dev_preprocess(pgd_graph *g, int neigh_kind, int s2l);
 pgd_status pgd_dev_cores(pgd_graph *g);
 pgd_status pgd_dev_assortativity(pgd_graph *g, double *r);
 pgd_status pgd_dev_sort_edges(pgd_graph *g, int order_kind, int s2l);
+pgd_status pgd_dev_sort_edges_sample(pgd_graph *g, int order_kind, int s2l, const int64_t *h_ids, int64_t k);
 pgd_status pgd_dev_micro_ids(pgd_graph *g, int64_t *d_src1, int64_t *d_dst1);
 
 // Decomposition (decompose.cu).

@@ -57,6 +57,9 @@ def lib():
         L.po_assortativity.argtypes = [_P]
         L.po_assortativity.restype = ctypes.c_double
         L.po_sort_edges.argtypes = [_P, ctypes.c_char_p, ctypes.c_int]
+        L.po_sort_edges_sample.argtypes = [_P, ctypes.c_char_p, ctypes.c_int, _I64P, ctypes.c_int64]
+        L.po_n_ord.restype = ctypes.c_int64
+        L.po_n_ord.argtypes = [_P]
         L.po_decompose.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.po_close.argtypes = [_U64P, ctypes.c_int64, ctypes.c_int64, _U64P]
         L.po_edge_sample.argtypes = [_P, ctypes.c_int64, _I64P, _I64P, _U64P, _U64P, _U64P, ctypes.c_int]
@@ -134,6 +137,23 @@ class OracleGraph:
             raise RuntimeError("decompose failed")
         return self
 
+    def run_sample(self, ids, neigh="deg", order="deg", s2l=False, micro=True, threads=0):
+        """preprocess, cores, sort_edges over the sampled edge ids, decompose"""
+        L = lib()
+        if L.po_preprocess(self.h, neigh.encode(), 0):
+            raise ValueError("preprocess failed")
+        L.po_compute_cores(self.h)
+        ids = np.ascontiguousarray(ids, np.int64)
+        if L.po_sort_edges_sample(self.h, order.encode(), int(s2l), ids, len(ids)):
+            raise ValueError("sort_edges (sample) failed")
+        if L.po_decompose(self.h, int(micro), threads, 0):
+            raise RuntimeError("decompose failed")
+        return self
+
+    @property
+    def n_ord(self):
+        return lib().po_n_ord(self.h)
+
     def prepare(self, neigh="deg", s2l_neigh=False, order="deg", s2l=False):
         """preprocess + cores + sort_edges, no decomposition"""
         L = lib()
@@ -172,9 +192,10 @@ class OracleGraph:
         return ev[: self.m], eu[: self.m]
 
     def order(self):
-        o = np.zeros(self.m + 1, np.int32)
+        k = self.n_ord
+        o = np.zeros(k + 1, np.int32)
         lib().po_get_order(self.h, o)
-        return o[: self.m]
+        return o[:k]
 
     def kcore(self):
         k = np.zeros(self.n + 1, np.int32)
@@ -199,7 +220,7 @@ class OracleGraph:
         return t
 
     def micro(self):
-        m = self.m
+        m = self.n_ord
         src = np.zeros(m + 1, np.int64)
         dst = np.zeros(m + 1, np.int64)
         cols = np.zeros((m + 1) * 8, np.uint64)
@@ -241,6 +262,10 @@ def ref_lib():
                                    ctypes.c_int, ctypes.c_char_p]
         R.ref_run.argtypes = [_P, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         R.ref_totals.argtypes = [_P, _U64P]
+        R.ref_run_ids.argtypes = [_P, ctypes.c_char_p, ctypes.c_int, _I64P, ctypes.c_longlong, ctypes.c_int,
+                                  ctypes.c_int]
+        R.ref_n_ord.restype = ctypes.c_int64
+        R.ref_n_ord.argtypes = [_P]
         R.ref_run_sample.restype = ctypes.c_longlong
         R.ref_run_sample.argtypes = [_P, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_longlong,
                                      ctypes.POINTER(ctypes.c_double)]
@@ -280,6 +305,11 @@ class RefGraph:
         ref_lib().ref_run(self.h, order.encode(), int(s2l), int(micro), workers)
         return self
 
+    def run_sample(self, ids, order="deg", s2l=False, micro=True, workers=1):
+        ids = np.ascontiguousarray(ids, np.int64)
+        ref_lib().ref_run_ids(self.h, order.encode(), int(s2l), ids, len(ids), int(micro), workers)
+        return self
+
     def time_sample(self, stride, order="deg", s2l=False, workers=1):
         sec = ctypes.c_double()
         k = ref_lib().ref_run_sample(self.h, order.encode(), int(s2l), workers, stride, ctypes.byref(sec))
@@ -307,7 +337,7 @@ class RefGraph:
         return t
 
     def micro(self):
-        m = self.m
+        m = ref_lib().ref_n_ord(self.h)
         src = np.zeros(m + 1, np.int64)
         dst = np.zeros(m + 1, np.int64)
         cols = np.zeros((m + 1) * 8, np.uint64)

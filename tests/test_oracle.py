@@ -223,3 +223,46 @@ def test_neighbour_orders_vs_reference(neigh, s2l):
     a, b, c = o.micro()
     x, y, w = r.micro()
     assert (a == x).all() and (b == y).all() and (c == w).all()
+
+
+def _sample_graph(seed):
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(60, 200))
+    k = int(rng.integers(3 * n, 8 * n))
+    src = rng.integers(0, n, k).astype(np.int32)
+    dst = rng.integers(0, n, k).astype(np.int32)
+    g = ol.OracleGraph.from_pairs(src, dst, dedup=True)
+    return g.csr(), rng
+
+
+@needs_ref
+@pytest.mark.parametrize("order,s2l", [("natural", False), ("deg", False), ("kcore", True), ("deg_vol", False)])
+def test_sampled_order_vs_reference(order, s2l):
+    """sort_edges with E_s (graphlet_core.cpp:836-851) then the decomposition:
+    the oracle's sampled path against the reference's, repeats included."""
+    (off, adj), rng = _sample_graph(31)
+    m = len(adj) // 2
+    ids = rng.integers(0, m, m // 3)
+    r = ol.RefGraph.from_csr(off, adj).run_sample(ids, order=order, s2l=s2l, micro=True)
+    o = ol.OracleGraph.from_csr(off, adj).run_sample(ids, order=order, s2l=s2l, micro=True)
+    assert o.n_ord == len(ids)
+    assert (o.totals() == r.totals()).all()
+    a, b, c = o.micro()
+    x, y, z = r.micro()
+    assert (a == x).all() and (b == y).all() and (c == z).all()
+
+
+def test_sampled_rows_equal_full_rows():
+    """A sampled edge's row does not depend on the sample: it equals the
+    edge's row in the full decomposition."""
+    (off, adj), rng = _sample_graph(32)
+    m = len(adj) // 2
+    full = ol.OracleGraph.from_csr(off, adj).run(order="natural", micro=True)
+    fs, fd, fc = full.micro()
+    rows = {(int(a), int(b)): c for a, b, c in zip(fs, fd, fc)}
+    ids = rng.choice(m, m // 2, replace=False)
+    o = ol.OracleGraph.from_csr(off, adj).run_sample(ids, order="kcore", micro=True)
+    s, d, c = o.micro()
+    assert len(c) == len(ids)
+    for a, b, row in zip(s, d, c):
+        assert (rows[(int(a), int(b))] == row).all()
