@@ -5,20 +5,24 @@
     python -m pgd_gb300.benchmarks large [--workloads rmat24,rgg24] [--samples 1000]
     python -m pgd_gb300.benchmarks profile [--scale 18] [--order kcore] [--reps 1]
     python -m pgd_gb300.benchmarks small [--reps 50]
+    python -m pgd_gb300.benchmarks profile_batch [--graphs 256]
 
 batch: 4096 independent graphs, n uniform in [16, 2048]; half G(n, p) with p
 uniform in [0.01, 0.5], half Barabasi-Albert with m uniform in {2..8}; all
 from one seed.  The thresholds are autotuned on a sample, then the whole set
 is decomposed in one call (one device build, one pass of the persistent
-kernels) and compared with the plain loop: one graph per call
-(pgd_graph_from_edges + pgd_decompose).  graphs/s for both.
+kernels) and compared with plain loops over a stratified sample, one graph
+per call: the single-graph API (pgd_graph_from_edges + pgd_decompose) with
+the default and with the tuned thresholds, and the batch kernels on a batch
+of one.  graphs/s for all; the speed-up is against the fastest plain loop.
 
 serve: requests arrive as a Poisson process of `rate` per second; each
 request's edge count is lognormal (median 5000, sigma 1.2, clipped at 50 M),
 half RMAT (scale ceil(log2(m/16)), edge factor chosen to hit m) and half
 G(n, p) with mean degree 16.  They go to the continuous-batching server;
 reported per offered rate: graphs/s, p50/p99 latency (submit to result),
-and the same request list through the plain one-graph-per-call loop.
+and the same request list through the plain one-graph-per-call loops (the
+single-graph API, and the batch kernels on a batch of one).
 
 large: RMAT scale 24 (edge factor 16, (a,b,c,d) = (0.57,0.19,0.19,0.05),
 seed 1) and the 3-D random geometric graph with n = 2^24 in the unit cube,
@@ -89,12 +93,22 @@ def plain_loop(ctx, graphs):
     return out, time.perf_counter() - t0
 
 
+def plain_batch1(ctx, graphs):
+    """One graph per call through the batch kernels (a batch of one)."""
+    out = []
+    t0 = time.perf_counter()
+    for s, d in graphs:
+        out.append(ctx.decompose_pairs_batch([(s, d)])[0].totals)
+    return out, time.perf_counter() - t0
+
+
 def run_batch(args):
     t0 = time.perf_counter()
     graphs, specs = batch_graphs(args.graphs, args.seed)
     pairs = sum(len(s) for s, _ in graphs)
     log("generated %d graphs, %d pairs in %.1fs" % (len(graphs), pairs, time.perf_counter() - t0))
     ctx = pgd.Context()
+    default_thr = ctx.thresholds()
     # autotune on a stratified sample (every 16th graph)
     sample = [ctx.graph_from_edges(s, d) for s, d in graphs[:: max(1, len(graphs) // 256)]]
     a, c, dm, ms = ctx.autotune(sample, reps=1)
@@ -110,17 +124,33 @@ def run_batch(args):
         res = ctx.decompose_pairs_batch(graphs)
         times.append(time.perf_counter() - t0)
     best = min(times)
-    # plain loop over an evenly spaced sample of the same graphs
+    # plain baselines over an evenly spaced sample of the same graphs, one graph
+    # per call: the single-graph API (with the default and with the tuned
+    # thresholds) and the batch kernels on a batch of one; the speed-up is
+    # quoted against the fastest of the three
     step = max(1, len(graphs) // max(1, args.plain_sample))
     idx = list(range(0, len(graphs), step))
-    plain, plain_s = plain_loop(ctx, [graphs[i] for i in idx])
-    mismatch = sum(int(not (p == res[i].totals).all()) for p, i in zip(plain, idx))
+    sub = [graphs[i] for i in idx]
     k = len(idx)
+    plain = {}
+    tuned_rate = None
+    p_t, s_t = plain_loop(ctx, sub)
+    plain["single_graph_api_tuned"] = k / s_t
+    ctx.set_thresholds(*default_thr)
+    p_d, s_d = plain_loop(ctx, sub)
+    plain["single_graph_api_default"] = k / s_d
+    ctx.set_thresholds(a, c, dm)
+    p_b, s_b = plain_batch1(ctx, sub)
+    plain["batch_of_one"] = k / s_b
+    mismatch = 0
+    for lst in (p_t, p_d, p_b):
+        mismatch += sum(int(not (p == res[i].totals).all()) for p, i in zip(lst, idx))
+    best_plain = max(plain.values())
     line = {
         "mode": "batch", "graphs": len(graphs), "pairs": pairs, "seconds": best, "graphs_per_s": len(graphs) / best,
         "kernel_ms": float(res[0].kernel_ms) if res else 0.0,
-        "plain_graphs": k, "plain_seconds": plain_s, "plain_graphs_per_s": k / plain_s,
-        "speedup_vs_plain": (len(graphs) / best) / (k / plain_s), "mismatches_vs_plain": mismatch,
+        "plain_graphs": k, "plain_graphs_per_s": plain, "speedup_vs_best_plain": (len(graphs) / best) / best_plain,
+        "mismatches_vs_plain": mismatch,
         "thresholds": {"anchor_hub": a, "cache_hub": c, "dense_max": dm},
         "workload": "4096 graphs, n~U[16,2048], half G(n,p) p~U[0.01,0.5], half BA m~U{2..8}, seed %d" % args.seed,
     }
@@ -180,13 +210,18 @@ def run_serve(args):
     reqs = serve_requests(args.requests, args.seed)
     pairs = sum(len(s) for s, _ in reqs)
     log("generated %d requests, %d pairs in %.1fs" % (len(reqs), pairs, time.perf_counter() - t0))
-    # plain loop first (also the expected counts)
+    # plain loops first (also the expected counts): one graph per call through
+    # the single-graph API and through the batch kernels (a batch of one)
     ctx = pgd.Context()
     plain_loop(ctx, reqs[:16])
     expect, plain_s = plain_loop(ctx, reqs)
+    plain_batch1(ctx, reqs[:16])
+    expect1, plain1_s = plain_batch1(ctx, reqs)
     ctx.close()
-    plain_rate = len(reqs) / plain_s
-    log("plain loop: %.1f graphs/s" % plain_rate)
+    assert all((x == y).all() for x, y in zip(expect, expect1))
+    plain_rates = {"single_graph_api": len(reqs) / plain_s, "batch_of_one": len(reqs) / plain1_s}
+    plain_rate = max(plain_rates.values())
+    log("plain loops: %s graphs/s" % plain_rates)
     # warm-up
     sv = pgd.Server(workers=args.workers)
     for s, d in reqs[:8]:
@@ -201,7 +236,7 @@ def run_serve(args):
             "mode": "serve", "requests": len(reqs), "pairs": pairs, "offered_rate": rate,
             "graphs_per_s": stats["graphs_per_s"], "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"],
             "mean_ms": stats["mean_ms"], "batches": stats["batches"], "wall_s": wall,
-            "plain_graphs_per_s": plain_rate, "speedup_vs_plain": stats["graphs_per_s"] / plain_rate,
+            "plain_graphs_per_s": plain_rates, "speedup_vs_best_plain": stats["graphs_per_s"] / plain_rate,
             "mismatches_vs_plain": mismatch, "workers": args.workers,
             "workload": "Poisson arrivals; m ~ lognormal(median 5000, sigma 1.2, <= 50M); half RMAT, half G(n,p) "
                         "mean degree 16; seed %d" % args.seed,
@@ -210,6 +245,17 @@ def run_serve(args):
 
 
 RMAT = dict(a=0.57, b=0.19, c=0.19)
+
+
+def run_profile_batch(args):
+    """The batched workload on its first `graphs` graphs (ncu captures of the
+    batch kernels on a small case)."""
+    graphs, _ = batch_graphs(args.graphs, args.seed)
+    ctx = pgd.Context()
+    ctx.set_thresholds(64, 128, 2048)
+    res = ctx.decompose_pairs_batch(graphs)
+    print(json.dumps({"mode": "profile_batch", "graphs": len(graphs), "pairs": sum(len(s) for s, _ in graphs),
+                      "kernel_ms": float(res[0].kernel_ms)}), flush=True)
 
 
 def run_profile(args):
@@ -324,7 +370,7 @@ def run_large(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("mode", choices=["batch", "serve", "large", "profile", "small"])
+    ap.add_argument("mode", choices=["batch", "serve", "large", "profile", "small", "profile_batch"])
     ap.add_argument("--workloads", default="rmat24,rgg24")
     ap.add_argument("--samples", type=int, default=1000)
     ap.add_argument("--heavy", type=int, default=10)
@@ -336,7 +382,7 @@ def main():
     ap.add_argument("--rates", default="", help="comma-separated offered rates to sweep (overrides --rate)")
     ap.add_argument("--workers", type=int, default=2)
     ap.add_argument("--reps", type=int, default=3)  # batch: timed repetitions; profile: decompositions
-    ap.add_argument("--plain-sample", type=int, default=128)
+    ap.add_argument("--plain-sample", type=int, default=256)
     ap.add_argument("--seed", type=int, default=1)
     args = ap.parse_args()
     if args.mode == "batch":
@@ -347,6 +393,8 @@ def main():
         run_large(args)
     elif args.mode == "small":
         run_small(args)
+    elif args.mode == "profile_batch":
+        run_profile_batch(args)
     else:
         run_profile(args)
 

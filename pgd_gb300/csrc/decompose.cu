@@ -1017,7 +1017,29 @@ __global__ void k_dense_bits(const int64_t *off, const int32_t *adj, const int32
     }
 }
 
-__global__ void __launch_bounds__(256) k_dense(DenseArgs A) {
+// q of a dense-graph edge: the endpoint of smaller degree (ties: v)
+__device__ __forceinline__ int32_t dense_q(const DevGraph &G, int64_t e) {
+    const int32_t id = G.order[e];
+    const int32_t v = G.ev[id], u = G.eu[id];
+    return G.deg[v] <= G.deg[u] ? v : u;
+}
+
+// Sort keys grouping the dense-graph edges by q (then by position), so that
+// k_dense can serve several edges with one pass over A_q's rows.
+__global__ void k_dense_keys(DevGraph G, const int32_t *dpos, int64_t nd, uint64_t *keys, int32_t *vals) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t e = dpos[i];
+        keys[i] = ((uint64_t)(uint32_t)dense_q(G, e) << 32) | (uint32_t)e;
+        vals[i] = e;
+    }
+}
+
+constexpr int kDenseGroup = 6;   // edges sharing q decomposed together
+
+// Up to kDenseGroup edges (p_j, q) with the same q: one pass over the rows of
+// A_q's neighbours w serves all of them -- row w is ANDed with S_p_j when
+// w is in S_q_j and with T_j when w is in T_j.
+__global__ void __launch_bounds__(256, 3) k_dense(DenseArgs A) {
     __shared__ unsigned long long s_red[8][PGD_NSUMS];
     const DevGraph &G = A.G;
     const int lane = threadIdx.x & 31;
@@ -1025,62 +1047,84 @@ __global__ void __launch_bounds__(256) k_dense(DenseArgs A) {
     unsigned long long acc[PGD_NSUMS];
 #pragma unroll
     for (int i = 0; i < PGD_NSUMS; i++) acc[i] = 0;
-    unsigned long long idx = 0, idx_end = 0;
     while (true) {
-        if (idx == idx_end) {
-            if (lane == 0) idx = atomicAdd(A.next, 4ull);
-            idx = __shfl_sync(0xffffffffu, idx, 0);
-            idx_end = min(idx + 4, (unsigned long long)A.ndense);
-        }
+        unsigned long long idx = 0;
+        if (lane == 0) idx = atomicAdd(A.next, (unsigned long long)kDenseGroup);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= (unsigned long long)A.ndense) break;
-        const int64_t e = A.dpos[idx++];
-        const int32_t id = G.order[e];
-        const int32_t v = G.ev[id], u = G.eu[id];
-        const int g = G.egraph[e];
-        const int64_t vb = A.vbase[g];
-        const int W = (int)((G.gnm[2 * g] + 63) >> 6);
-        const uint64_t *rows = A.bits + A.wbase[g];
-        // scan the endpoint of smaller degree: |S_q| + t = d_q - 1 rows
-        const bool vq = G.deg[v] <= G.deg[u];
-        const int64_t q = (vq ? v : u) - vb, p = (vq ? u : v) - vb;
-        const uint64_t Ap = lane < W ? __ldg(rows + p * W + lane) : 0ull;
-        const uint64_t Aq = lane < W ? __ldg(rows + q * W + lane) : 0ull;
-        const uint64_t bq = (lane == (int)(q >> 6)) ? (1ull << (q & 63)) : 0ull;
-        const uint64_t bp = (lane == (int)(p >> 6)) ? (1ull << (p & 63)) : 0ull;
-        const uint64_t T = Ap & Aq;
-        const uint64_t Sp = Ap & ~Aq & ~bq;
-        const uint64_t Sq = Aq & ~Ap & ~bp;
-        unsigned long long t = __popcll(T), c4 = 0, k4x2 = 0;
-        for (int L = 0; L < W; L++) {
-            uint64_t ws = __shfl_sync(0xffffffffu, Sq, L);
-            uint64_t wt = __shfl_sync(0xffffffffu, T, L);
-            while (ws) {
-                const int b0 = __ffsll(ws) - 1;
-                ws &= ws - 1;
-                const int64_t w0 = (int64_t)L * 64 + b0;
-                if (ws) {
-                    const int b1 = __ffsll(ws) - 1;
-                    ws &= ws - 1;
-                    const int64_t w1 = (int64_t)L * 64 + b1;
-                    const uint64_t r0 = lane < W ? __ldg(rows + w0 * W + lane) : 0ull;
-                    const uint64_t r1 = lane < W ? __ldg(rows + w1 * W + lane) : 0ull;
-                    c4 += __popcll(r0 & Sp) + __popcll(r1 & Sp);
-                } else {
-                    const uint64_t r0 = lane < W ? __ldg(rows + w0 * W + lane) : 0ull;
-                    c4 += __popcll(r0 & Sp);
+        const int64_t iend = min(idx + (unsigned long long)kDenseGroup, (unsigned long long)A.ndense);
+        int64_t i0 = (int64_t)idx;
+        while (i0 < iend) {
+            // the run of edges with the same q (dpos is grouped by q)
+            const int32_t qg = dense_q(G, A.dpos[i0]);
+            int64_t i1 = i0 + 1;
+            while (i1 < iend && dense_q(G, A.dpos[i1]) == qg) i1++;
+            const int R = (int)(i1 - i0);
+            const int g = G.egraph[A.dpos[i0]];
+            const int64_t vb = A.vbase[g];
+            const int W = (int)((G.gnm[2 * g] + 63) >> 6);
+            const uint64_t *rows = A.bits + A.wbase[g];
+            const int64_t q = qg - vb;
+            const uint64_t Aq = lane < W ? __ldg(rows + q * W + lane) : 0ull;
+            const uint64_t bq = (lane == (int)(q >> 6)) ? (1ull << (q & 63)) : 0ull;
+            uint64_t T[kDenseGroup], Sp[kDenseGroup], Sq[kDenseGroup];
+            unsigned c4[kDenseGroup], k4x2[kDenseGroup];
+#pragma unroll
+            for (int j = 0; j < kDenseGroup; j++) {
+                T[j] = Sp[j] = Sq[j] = 0;
+                c4[j] = k4x2[j] = 0;
+                if (j < R) {
+                    const int32_t id = G.order[A.dpos[i0 + j]];
+                    const int32_t v = G.ev[id], u = G.eu[id];
+                    const int64_t p = (v == qg ? u : v) - vb;
+                    const uint64_t Ap = lane < W ? __ldg(rows + p * W + lane) : 0ull;
+                    const uint64_t bp = (lane == (int)(p >> 6)) ? (1ull << (p & 63)) : 0ull;
+                    T[j] = Ap & Aq;
+                    Sp[j] = Ap & ~Aq & ~bq;
+                    Sq[j] = Aq & ~Ap & ~bp;
                 }
             }
-            while (wt) {
-                const int b0 = __ffsll(wt) - 1;
-                wt &= wt - 1;
-                const uint64_t r0 = lane < W ? __ldg(rows + ((int64_t)L * 64 + b0) * W + lane) : 0ull;
-                k4x2 += __popcll(r0 & T);
+            for (int L = 0; L < W; L++) {
+                uint64_t wq = __shfl_sync(0xffffffffu, Aq, L);
+                uint64_t ws[kDenseGroup], wt[kDenseGroup];
+#pragma unroll
+                for (int j = 0; j < kDenseGroup; j++) {
+                    ws[j] = __shfl_sync(0xffffffffu, Sq[j], L);
+                    wt[j] = __shfl_sync(0xffffffffu, T[j], L);
+                }
+                while (wq) {
+                    const int b0 = __ffsll(wq) - 1;
+                    wq &= wq - 1;
+                    int b1 = -1;
+                    if (wq) {
+                        b1 = __ffsll(wq) - 1;
+                        wq &= wq - 1;
+                    }
+                    const uint64_t r0 = lane < W ? __ldg(rows + ((int64_t)L * 64 + b0) * W + lane) : 0ull;
+                    const uint64_t r1 = (b1 >= 0 && lane < W) ? __ldg(rows + ((int64_t)L * 64 + b1) * W + lane) : 0ull;
+#pragma unroll
+                    for (int j = 0; j < kDenseGroup; j++) {
+                        if ((ws[j] >> b0) & 1ull) c4[j] += __popcll(r0 & Sp[j]);
+                        else if ((wt[j] >> b0) & 1ull) k4x2[j] += __popcll(r0 & T[j]);
+                        if (b1 >= 0) {
+                            if ((ws[j] >> b1) & 1ull) c4[j] += __popcll(r1 & Sp[j]);
+                            else if ((wt[j] >> b1) & 1ull) k4x2[j] += __popcll(r1 & T[j]);
+                        }
+                    }
+                }
             }
+#pragma unroll
+            for (int j = 0; j < kDenseGroup; j++) {
+                if (j >= R) break;
+                const unsigned long long t = pgd_warp_sum(__popcll(T[j]));
+                const unsigned long long c = pgd_warp_sum(c4[j]);
+                const unsigned long long k2 = pgd_warp_sum(k4x2[j]);
+                const int64_t e = A.dpos[i0 + j];
+                const int32_t id = G.order[e];
+                edge_epilogue(G, acc, cur_g, e, G.ev[id], G.eu[id], t, k2 >> 1, c, lane);
+            }
+            i0 = i1;
         }
-        t = pgd_warp_sum(t);
-        c4 = pgd_warp_sum(c4);
-        k4x2 = pgd_warp_sum(k4x2);
-        edge_epilogue(G, acc, cur_g, e, v, u, t, k4x2 >> 1, c4, lane);
     }
     block_flush(G, acc, cur_g, s_red, 8);
 }
@@ -1359,6 +1403,14 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
         PGD_LAUNCH(ctx, k_hub, nsm, kHubWarps * 32, smem, H);
     }
     if (nd > 0 && dense) {
+        // dense edges grouped by q, so that k_dense serves several per row pass
+        PGD_LAUNCH(ctx, k_dense_keys, grid_for(nd), kThreads, 0, G, posv + nh, (int64_t)nd, keys, vals);
+        size_t tbd = 0;
+        void *tmpd = nullptr;
+        cub::DeviceRadixSort::SortPairs(nullptr, tbd, keys, keys2, vals, posv + nh, (int64_t)nd, 0, 64, s);
+        if ((st = pgd_tmp_alloc(ctx, &tmpd, tbd))) return st;
+        cub::DeviceRadixSort::SortPairs(tmpd, tbd, keys, keys2, vals, posv + nh, (int64_t)nd, 0, 64, s);
+        pgd_tmp_free(ctx, tmpd);
         DenseArgs D;
         D.G = G;
         D.bits = dense->bits;
