@@ -213,54 +213,6 @@ __global__ void k_core_init(const int32_t *deg, int64_t n, int32_t *cur, int32_t
     }
 }
 
-// Start of a level: every alive vertex with cur <= level leaves now; also the
-// smallest cur among the rest (to skip empty levels) and how many are alive.
-__global__ void k_core_level(int32_t *cur, int32_t *core, int64_t n, int level, int32_t *frontier,
-                             unsigned int *fsize, int *min_rest, unsigned int *alive) {
-    int local_min = INT_MAX;
-    unsigned int local_alive = 0;
-    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-        if (core[v] != -1) continue;
-        int c = cur[v];
-        if (c <= level) {
-            core[v] = level;
-            frontier[atomicAdd(fsize, 1u)] = (int32_t)v;
-        } else {
-            local_min = min(local_min, c);
-            local_alive++;
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        local_min = min(local_min, __shfl_xor_sync(0xffffffffu, local_min, o));
-        local_alive += __shfl_xor_sync(0xffffffffu, local_alive, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        if (local_min != INT_MAX) atomicMin(min_rest, local_min);
-        if (local_alive) atomicAdd(alive, local_alive);
-    }
-}
-
-// Remove the frontier: each alive neighbour loses one; the one whose count
-// drops to `level` joins the next frontier.  One warp per frontier vertex.
-__global__ void k_core_peel(const int64_t *off, const int32_t *adj, int32_t *cur, int32_t *core, int level,
-                            const int32_t *frontier, unsigned int fsize, int32_t *next, unsigned int *nsize) {
-    int lane = threadIdx.x & 31;
-    int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t f = w; f < fsize; f += nw) {
-        int32_t v = frontier[f];
-        for (int64_t j = off[v] + lane; j < off[v + 1]; j += 32) {
-            int32_t x = adj[j];
-            if (core[x] != -1) continue;
-            int old = atomicSub(&cur[x], 1);
-            if (old == level + 1) {
-                core[x] = level;
-                next[atomicAdd(nsize, 1u)] = x;
-            }
-        }
-    }
-}
-
 __global__ void k_max_core(const int32_t *core, int64_t n_minus_1, int *out) {
     int local = 0;
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n_minus_1; v += (int64_t)gridDim.x * blockDim.x)
@@ -603,6 +555,103 @@ pgd_status pgd_dev_preprocess(pgd_graph *g, int neigh_kind, int s2l) {
     return PGD_OK;
 }
 
+// Device-driven peeling: the state machine below replaces a host loop with
+// one round trip per level and per peel round.  Each step is a work kernel
+// (a level scan or a peel round, chosen from the state) and a one-thread
+// control kernel that applies the transition; a block of kCoreSteps steps is
+// captured once as a CUDA graph and replayed until the control kernel
+// reports that every vertex has a core number.
+namespace {
+
+struct CoreState {
+    int level, mode, sel, done, failed, min_rest;
+    unsigned int cnt[2];          // frontier sizes of buffers 0 and 1
+    long long removed, steps, max_steps;
+};
+
+constexpr int kCoreSteps = 64;
+enum { kCoreScan = 0, kCorePeel = 1 };
+
+__global__ void k_core_work(const int64_t *off, const int32_t *adj, int32_t *cur, int32_t *core, int64_t n,
+                            int32_t *f0, int32_t *f1, CoreState *st) {
+    if (st->done) return;
+    const int mode = st->mode, level = st->level, sel = st->sel;
+    int32_t *fin = sel ? f1 : f0, *fout = sel ? f0 : f1;
+    if (mode == kCoreScan) {
+        // every alive vertex with cur <= level leaves now; the smallest cur
+        // among the rest lets the control kernel skip empty levels
+        int local_min = INT_MAX;
+        for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+            if (core[v] != -1) continue;
+            const int c = cur[v];
+            if (c <= level) {
+                core[v] = level;
+                fin[atomicAdd(&st->cnt[sel], 1u)] = (int32_t)v;
+            } else {
+                local_min = min(local_min, c);
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) local_min = min(local_min, __shfl_xor_sync(0xffffffffu, local_min, o));
+        if ((threadIdx.x & 31) == 0 && local_min != INT_MAX) atomicMin(&st->min_rest, local_min);
+    } else {
+        // remove the frontier: each alive neighbour loses one; the one whose
+        // count drops to `level` joins the next frontier (one warp per vertex)
+        const int lane = threadIdx.x & 31;
+        const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+        const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+        const unsigned int fsize = st->cnt[sel];
+        for (int64_t f = w; f < fsize; f += nw) {
+            const int32_t v = fin[f];
+            for (int64_t j = off[v] + lane; j < off[v + 1]; j += 32) {
+                const int32_t x = adj[j];
+                if (core[x] != -1) continue;
+                const int old = atomicSub(&cur[x], 1);
+                if (old == level + 1) {
+                    core[x] = level;
+                    fout[atomicAdd(&st->cnt[sel ^ 1], 1u)] = x;
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_core_ctrl(CoreState *st, int64_t n) {
+    if (st->done) return;
+    const int sel = st->sel;
+    if (st->mode == kCoreScan) {
+        const unsigned int f = st->cnt[sel];
+        if (f == 0) {
+            // nobody at this level: jump to the smallest remaining count
+            st->level = max(st->level + 1, st->min_rest);
+            st->min_rest = INT_MAX;
+        } else {
+            st->removed += f;
+            st->mode = kCorePeel;
+            st->cnt[sel ^ 1] = 0;
+        }
+    } else {
+        const unsigned int nf = st->cnt[sel ^ 1];
+        st->removed += nf;
+        if (nf == 0) {
+            st->level += 1;
+            st->mode = kCoreScan;
+            st->cnt[sel] = 0;
+            st->min_rest = INT_MAX;
+        } else {
+            st->sel = sel ^ 1;
+            st->cnt[sel] = 0;   // the buffer written next
+        }
+    }
+    st->steps += 1;
+    if (st->removed >= n) st->done = 1;
+    else if (st->steps >= st->max_steps) {
+        st->done = 1;
+        st->failed = 1;
+    }
+}
+
+}  // namespace
+
 pgd_status pgd_dev_cores(pgd_graph *g) {
     pgd_ctx *ctx = g->ctx;
     cudaStream_t s = ctx->stream;
@@ -613,56 +662,70 @@ pgd_status pgd_dev_cores(pgd_graph *g) {
     }
     if (n == 0) { g->has_cores = true; g->max_core = 0; return PGD_OK; }
     int32_t *cur = nullptr, *fa = nullptr, *fb = nullptr;
-    unsigned int *cnt = nullptr;  // [0] frontier size, [1] next size, [2] alive, [3] min_rest
+    CoreState *d_st = nullptr;
     if ((st = pgd_tmp_alloc(ctx, (void **)&cur, n * sizeof(int32_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&fa, n * sizeof(int32_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&fb, n * sizeof(int32_t)))) return st;
-    if ((st = pgd_tmp_alloc(ctx, (void **)&cnt, 8 * sizeof(unsigned int)))) return st;
+    if ((st = pgd_tmp_alloc(ctx, (void **)&d_st, sizeof(CoreState)))) return st;
+    auto release = [&]() {
+        pgd_tmp_free(ctx, cur);
+        pgd_tmp_free(ctx, fa);
+        pgd_tmp_free(ctx, fb);
+        pgd_tmp_free(ctx, d_st);
+    };
     PGD_LAUNCH(ctx, k_core_init, grid_for(n), kThreads, 0, g->deg, n, cur, g->core);
-    int level = 0;
-    int64_t removed = 0;
-    unsigned int h[4];
-    int peel_grid = grid_for(32 * (int64_t)ctx->num_sms * 64);
-    while (removed < n) {
-        if (level > g->max_degree + 1) {
-            pgd_tmp_free(ctx, cur); pgd_tmp_free(ctx, fa); pgd_tmp_free(ctx, fb); pgd_tmp_free(ctx, cnt);
-            return pgd_fail(ctx, PGD_EINVAL, "k-core peeling did not converge");
+    // every step removes a vertex or raises the level (at most max_degree + 1
+    // levels), so 2 (n + max_degree) + 4 steps always suffice
+    CoreState h{};
+    h.min_rest = INT_MAX;
+    h.max_steps = 2 * (n + (long long)g->max_degree) + 4;
+    PGD_CUDA(ctx, cudaMemcpyAsync(d_st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+    const int work_grid = grid_for(32 * (int64_t)ctx->num_sms * 64);
+    // capture kCoreSteps steps once, replay until done
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        for (int i = 0; i < kCoreSteps; i++) {
+            k_core_work<<<work_grid, kThreads, 0, s>>>(g->off, g->adj, cur, g->core, n, fa, fb, d_st);
+            k_core_ctrl<<<1, 1, 0, s>>>(d_st, n);
         }
-        PGD_CUDA(ctx, cudaMemsetAsync(cnt, 0, 4 * sizeof(unsigned int), s));
-        PGD_CUDA(ctx, cudaMemsetAsync(cnt + 3, 0x7f, sizeof(unsigned int), s));
-        PGD_LAUNCH(ctx, k_core_level, grid_for(n), kThreads, 0, cur, g->core, n, level, fa, cnt, (int *)(cnt + 3), cnt + 2);
-        PGD_CUDA(ctx, cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s));
-        PGD_CUDA(ctx, cudaStreamSynchronize(s));
-        unsigned int fsize = h[0];
-        if (fsize == 0) {
-            // nobody sits at this level; h[3] is the smallest remaining count
-            // and the state has not changed since it was taken
-            level = std::max(level + 1, (int)h[3]);
-            continue;
-        }
-        removed += fsize;
-        while (fsize > 0) {
-            PGD_CUDA(ctx, cudaMemsetAsync(cnt + 1, 0, sizeof(unsigned int), s));
-            PGD_LAUNCH(ctx, k_core_peel, peel_grid, kThreads, 0, g->off, g->adj, cur, g->core, level, fa, fsize, fb, cnt + 1);
-            unsigned int nsize = 0;
-            PGD_CUDA(ctx, cudaMemcpyAsync(&nsize, cnt + 1, sizeof(nsize), cudaMemcpyDeviceToHost, s));
-            PGD_CUDA(ctx, cudaStreamSynchronize(s));
-            removed += nsize;
-            std::swap(fa, fb);
-            fsize = nsize;
-        }
-        level++;
+        e = cudaStreamEndCapture(s, &graph);
     }
-    int *d_mc = (int *)cnt;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        release();
+        return pgd_cuda_fail(ctx, e, "k-core step graph");
+    }
+    int done = 0;
+    while (!done) {
+        e = cudaGraphLaunch(exec, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&done, &d_st->done, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) break;
+        ctx->launches += 2 * kCoreSteps;
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        release();
+        return pgd_cuda_fail(ctx, e, "k-core peeling");
+    }
+    PGD_CUDA(ctx, cudaMemcpyAsync(&h, d_st, sizeof(h), cudaMemcpyDeviceToHost, s));
+    int *d_mc = (int *)d_st;
+    PGD_CUDA(ctx, cudaStreamSynchronize(s));
+    if (h.failed) {
+        release();
+        return pgd_fail(ctx, PGD_EINVAL, "k-core peeling did not converge");
+    }
     PGD_CUDA(ctx, cudaMemsetAsync(d_mc, 0, sizeof(int), s));
     if (n > 1) PGD_LAUNCH(ctx, k_max_core, grid_for(n - 1), kThreads, 0, g->core, n - 1, d_mc);
     int mc = 0;
     PGD_CUDA(ctx, cudaMemcpyAsync(&mc, d_mc, sizeof(int), cudaMemcpyDeviceToHost, s));
     PGD_CUDA(ctx, cudaStreamSynchronize(s));
-    pgd_tmp_free(ctx, cur);
-    pgd_tmp_free(ctx, fa);
-    pgd_tmp_free(ctx, fb);
-    pgd_tmp_free(ctx, cnt);
+    release();
     PGD_CUDA(ctx, cudaGetLastError());
     g->max_core = mc;
     g->has_cores = true;
