@@ -64,6 +64,7 @@ constexpr int kMaxChunks = 8;            // ... but an anchor is split into at m
                                          // every item rebuilds the anchor's bitmap and W histogram
 constexpr int kMaxDynSmem = 156 * 1024;  // k_hub dynamic shared memory: bitmap, then the W histogram
 constexpr int kMaxTslotSmem = 200 * 1024;  // k_tslot_hub dynamic shared memory: rank bitmap
+constexpr int kTHigh = 4096;             // T members of rank >= kRankBits listed per warp (beyond: search N(q))
 constexpr int kRankBits = 16384;         // T members of degree rank below this are marked in a per-warp bitmap;
                                          // vertices of rank below this get a rank-bitmap row of N+(x)
 
@@ -459,6 +460,7 @@ struct HubArgs {
     int32_t split;            // ranks below this are kept in shared memory
     unsigned long long *next;
     int4 *slot_out;           // k_tslot_hub: slot records whose t it writes
+    int32_t *thigh;           // k_hub: per-warp lists of T's high-rank members (kTHigh each)
 };
 
 // |{r in L[0..len) : r in N(p)}| for a list of ranks, warp-cooperative,
@@ -487,10 +489,18 @@ __device__ __forceinline__ unsigned row_and_count(const uint32_t *row, const uin
 // T's members of degree rank < kRankBits are marked in a per-warp bitmap and
 // the test is one shared-memory bit; other y fall back to the N(p) bitmap and
 // a search of N(q).
+// T's members of rank >= kRankBits, in id order, kept by the warp in pass 1
+// (a per-warp global slice that stays in L1) when there are at most kTHigh.
+struct THigh {
+    const int32_t *ids;
+    int count;       // -1: more than kTHigh, search N(q) instead
+};
+
 __device__ __forceinline__ bool in_t(const uint32_t *Rw, const RankBits &bm, const int32_t *Nq, int dq, int32_t y,
-                                     int32_t ry) {
+                                     int32_t ry, const THigh &th) {
     if (ry < kRankBits) return (Rw[ry >> 5] >> (ry & 31)) & 1u;
-    return bm.test(ry) && pgd_contains(Nq, dq, y);
+    if (!bm.test(ry)) return false;
+    return th.count >= 0 ? pgd_contains(th.ids, th.count, y) : pgd_contains(Nq, dq, y);
 }
 
 // Histogram of the hub ids in the lists of the 32 vertices the warp holds
@@ -666,6 +676,7 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
             unsigned long long sumtq = 0, sumW = 0, k4 = 0;
             int len0 = 0, kind0 = 0;
             const int32_t *list0 = nullptr, *rlist0 = nullptr;
+            int nhigh = A.thigh ? 0 : -1;   // T members of rank >= kRankBits listed so far (warp-uniform)
             for (int base = 0; base < dq; base += 64) {
                 const int j0 = base + lane, j1 = base + 32 + lane;
                 const int4 none = make_int4(p, 0, -1, 0);
@@ -674,13 +685,14 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
 #pragma unroll
                 for (int h2 = 0; h2 < 2; h2++) {
                     const int4 sr = h2 ? s1 : s0;
-                    bool inT = false;
+                    bool inT = false, hi = false;
                     if (sr.x != p) {
                         inT = bm.test(sr.y & 0x7fffffff);
                         if (inT) {
                             sumtq += (uint32_t)sr.w;
                             const int32_t r = sr.y & 0x7fffffff;
                             if (r < kRankBits) atomicOr(Rw + (r >> 5), 1u << (r & 31));
+                            hi = r >= kRankBits;
                         } else {
                             const int32_t h = sr.z;
                             if (h >= 0) sumW += hval(smem_hist ? sh_hist[hw(h)] : __ldcg(gl_hist + hw(h)), h);
@@ -688,9 +700,22 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                         if (dq <= 32 && h2 == 0) plan_entry(G, inT, sr, len0, kind0, list0, rlist0);
                     }
                     t += __popc(__ballot_sync(0xffffffffu, inT));
+                    // list T's high-rank members in N(q)'s (id) order
+                    const unsigned hm = __ballot_sync(0xffffffffu, hi);
+                    if (hm && nhigh >= 0) {
+                        const int at = nhigh + __popc(hm & ((1u << lane) - 1));
+                        if (nhigh + __popc(hm) > kTHigh) nhigh = -1;
+                        else {
+                            if (hi) A.thigh[(int64_t)(blockIdx.x * kHubWarps + wid) * kTHigh + at] = sr.x;
+                            nhigh += __popc(hm);
+                        }
+                    }
                 }
             }
             __syncwarp();
+            THigh th;
+            th.ids = A.thigh ? A.thigh + (int64_t)(blockIdx.x * kHubWarps + wid) * kTHigh : nullptr;
+            th.count = nhigh;
             // pass 2: N(w) of non-hub w in S_q (kind 0), N+(x) of x in T as a
             // list (kind 1) or as a rank-bitmap row (kind 2)
             for (int base = 0; base < dq; base += 32) {
@@ -725,9 +750,9 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                         for (; i + 32 < ln; i += 64) {
                             const int32_t y0 = __ldg(L + i), y1 = __ldg(L + i + 32);
                             const int32_t r0 = __ldg(LR + i), r1 = __ldg(LR + i + 32);
-                            k4 += (in_t(Rw, bm, Nq, dq, y0, r0) ? 1 : 0) + (in_t(Rw, bm, Nq, dq, y1, r1) ? 1 : 0);
+                            k4 += (in_t(Rw, bm, Nq, dq, y0, r0, th) ? 1 : 0) + (in_t(Rw, bm, Nq, dq, y1, r1, th) ? 1 : 0);
                         }
-                        for (; i < ln; i += 32) k4 += in_t(Rw, bm, Nq, dq, __ldg(L + i), __ldg(LR + i)) ? 1 : 0;
+                        for (; i < ln; i += 32) k4 += in_t(Rw, bm, Nq, dq, __ldg(L + i), __ldg(LR + i), th) ? 1 : 0;
                     }
                 }
                 // short lists: flattened over the warp
@@ -753,12 +778,12 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                     if (vA) {
                         if (okA == 0) sumW += bm.test(xA);
                         else if (okA == 2) k4 += __popc((uint32_t)xA & Rw[idxA]);
-                        else k4 += in_t(Rw, bm, Nq, dq, xA, rA) ? 1 : 0;
+                        else k4 += in_t(Rw, bm, Nq, dq, xA, rA, th) ? 1 : 0;
                     }
                     if (vB) {
                         if (okB == 0) sumW += bm.test(xB);
                         else if (okB == 2) k4 += __popc((uint32_t)xB & Rw[idxB]);
-                        else k4 += in_t(Rw, bm, Nq, dq, xB, rB) ? 1 : 0;
+                        else k4 += in_t(Rw, bm, Nq, dq, xB, rB, th) ? 1 : 0;
                     }
                 }
             }
@@ -1318,6 +1343,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     uint32_t *ghist = nullptr;
     uint32_t *gbm = nullptr;
     int2 *hrec = nullptr;
+    int32_t *thigh = nullptr;
     if ((st = pgd_tmp_alloc(ctx, (void **)&keys, m * sizeof(uint64_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&keys2, m * sizeof(uint64_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&posv, m * sizeof(int32_t)))) return st;
@@ -1392,6 +1418,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
         if (!H.smem_hist) {
             if ((st = pgd_tmp_alloc(ctx, (void **)&ghist, (size_t)nsm * H.hstride * 4))) return st;
         }
+        if ((st = pgd_tmp_alloc(ctx, (void **)&thigh, (size_t)nsm * kHubWarps * kTHigh * sizeof(int32_t)))) return st;
         PGD_CUDA(ctx, cudaFuncSetAttribute(k_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         H.G = G;
         H.hpos = posv;
@@ -1401,6 +1428,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
         H.ghist = ghist;
         H.gbitmap = gbm;
         H.next = ctr + 1;
+        H.thigh = thigh;
         PGD_LAUNCH(ctx, k_hub, nsm, kHubWarps * 32, smem, H);
     }
     if (nd > 0 && dense) {
@@ -1442,6 +1470,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     pgd_tmp_free(ctx, ghist);
     pgd_tmp_free(ctx, gbm);
     pgd_tmp_free(ctx, hrec);
+    pgd_tmp_free(ctx, thigh);
     PGD_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
     PGD_CUDA(ctx, cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
     return PGD_OK;
@@ -2001,6 +2030,7 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
         H.ghist = ghist;
         H.gbitmap = gbm;
         H.next = ctr + 1;
+        H.thigh = nullptr;   // membership beyond the rank bitmap by searching N(q)
         k_hub<<<nsm, kHubWarps * 32, smem, s>>>(H);
     }
     const int64_t nlight = m - (int64_t)nh;
