@@ -1159,6 +1159,29 @@ __global__ void __launch_bounds__(256, 3) k_dense(DenseArgs A) {
 
 // ---------------------------------------------------------------------------
 
+// Stream-ordered temporaries released on every return path (also when an
+// allocation or a CUDA call fails half-way).
+struct TmpGuard {
+    pgd_ctx *ctx;
+    std::vector<void *> held;
+    explicit TmpGuard(pgd_ctx *c) : ctx(c) {}
+    TmpGuard(const TmpGuard &) = delete;
+    TmpGuard &operator=(const TmpGuard &) = delete;
+    ~TmpGuard() {
+        for (void *p : held) pgd_tmp_free(ctx, p);
+    }
+    template <typename T>
+    pgd_status alloc(T **out, size_t bytes) {
+        void *p = nullptr;
+        const pgd_status st = pgd_tmp_alloc(ctx, &p, bytes);
+        if (st == PGD_OK) {
+            held.push_back(p);
+            *out = (T *)p;
+        }
+        return st;
+    }
+};
+
 static pgd_status build_aux(pgd_graph *g) {
     pgd_ctx *ctx = g->ctx;
     cudaStream_t s = ctx->stream;
@@ -1178,12 +1201,13 @@ static pgd_status build_aux(pgd_graph *g) {
         g->top_words = top_row_base(g->top_r);
         if ((st = pgd_graph_alloc(g, (void **)&g->toprows, (g->top_words + 1) * sizeof(uint32_t)))) return st;
     }
+    TmpGuard tg(ctx);
     int32_t *row = nullptr;
     uint32_t *flag = nullptr, *pos = nullptr;
     const int64_t len = std::max(nnz, n) + 1;
-    if ((st = pgd_tmp_alloc(ctx, (void **)&row, (nnz + 1) * sizeof(int32_t)))) return st;
-    if ((st = pgd_tmp_alloc(ctx, (void **)&flag, len * sizeof(uint32_t)))) return st;
-    if ((st = pgd_tmp_alloc(ctx, (void **)&pos, len * sizeof(uint32_t)))) return st;
+    if ((st = tg.alloc(&row, (nnz + 1) * sizeof(int32_t)))) return st;
+    if ((st = tg.alloc(&flag, len * sizeof(uint32_t)))) return st;
+    if ((st = tg.alloc(&pos, len * sizeof(uint32_t)))) return st;
     void *tmp = nullptr;
     size_t tb = 0;
     // oriented lists
@@ -1229,8 +1253,8 @@ static pgd_status build_aux(pgd_graph *g) {
     // degree ranks of the vertices and of the oriented list entries
     {
         uint64_t *rk = nullptr, *rk2 = nullptr;
-        if ((st = pgd_tmp_alloc(ctx, (void **)&rk, (n + 1) * sizeof(uint64_t)))) return st;
-        if ((st = pgd_tmp_alloc(ctx, (void **)&rk2, (n + 1) * sizeof(uint64_t)))) return st;
+        if ((st = tg.alloc(&rk, (n + 1) * sizeof(uint64_t)))) return st;
+        if ((st = tg.alloc(&rk2, (n + 1) * sizeof(uint64_t)))) return st;
         if (n > 0) {
             PGD_LAUNCH(ctx, k_rank_keys, grid_for(n), kThreads, 0, g->deg, n, rk);
             tb = 0;
@@ -1244,8 +1268,6 @@ static pgd_status build_aux(pgd_graph *g) {
             PGD_LAUNCH(ctx, k_gather_rank, grid_for(g->m), kThreads, 0, g->adjp, g->vrank, g->m, g->adjp_rank);
             PGD_LAUNCH(ctx, k_gather_rank, grid_for(nnz), kThreads, 0, g->adj, g->vrank, nnz, g->adj_rank);
         }
-        pgd_tmp_free(ctx, rk);
-        pgd_tmp_free(ctx, rk2);
     }
     if (n > 0)
         PGD_LAUNCH(ctx, k_vrec, grid_for(n), kThreads, 0, g->off, g->offp, g->deg, g->vrank, g->hubid, n,
@@ -1261,9 +1283,6 @@ static pgd_status build_aux(pgd_graph *g) {
                    g->toprows);
     PGD_CUDA(ctx, cudaStreamSynchronize(s));
     g->nhubs = (int32_t)nh;
-    pgd_tmp_free(ctx, row);
-    pgd_tmp_free(ctx, flag);
-    pgd_tmp_free(ctx, pos);
     PGD_CUDA(ctx, cudaGetLastError());
     g->aux_cache_hub = ctx->cache_hub;
     g->has_aux = true;
@@ -1344,10 +1363,11 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     uint32_t *gbm = nullptr;
     int2 *hrec = nullptr;
     int32_t *thigh = nullptr;
-    if ((st = pgd_tmp_alloc(ctx, (void **)&keys, m * sizeof(uint64_t)))) return st;
-    if ((st = pgd_tmp_alloc(ctx, (void **)&keys2, m * sizeof(uint64_t)))) return st;
-    if ((st = pgd_tmp_alloc(ctx, (void **)&posv, m * sizeof(int32_t)))) return st;
-    if ((st = pgd_tmp_alloc(ctx, (void **)&vals, m * sizeof(int32_t)))) return st;
+    TmpGuard tg(ctx);
+    if ((st = tg.alloc(&keys, m * sizeof(uint64_t)))) return st;
+    if ((st = tg.alloc(&keys2, m * sizeof(uint64_t)))) return st;
+    if ((st = tg.alloc(&posv, m * sizeof(int32_t)))) return st;
+    if ((st = tg.alloc(&vals, m * sizeof(int32_t)))) return st;
     // [0] hub edges, [1] hub item counter, [2] light counter, [3] dense edges, [4] dense counter
     unsigned long long *ctr = ctx->d_ctr;
     PGD_CUDA(ctx, cudaMemsetAsync(ctr, 0, 8 * sizeof(unsigned long long), s));
@@ -1366,8 +1386,8 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     const int64_t nlight = m - (int64_t)nh - (int64_t)nd;
     int64_t nitems = 0;
     if (nh > 0) {
-        if ((st = pgd_tmp_alloc(ctx, (void **)&flag, (nh + 1) * sizeof(uint32_t)))) return st;
-        if ((st = pgd_tmp_alloc(ctx, (void **)&fpos, (nh + 1) * sizeof(uint32_t)))) return st;
+        if ((st = tg.alloc(&flag, (nh + 1) * sizeof(uint32_t)))) return st;
+        if ((st = tg.alloc(&fpos, (nh + 1) * sizeof(uint32_t)))) return st;
         PGD_LAUNCH(ctx, k_item_flags, grid_for(nh), kThreads, 0, keys2, (int64_t)nh, flag);
         PGD_CUDA(ctx, cudaMemsetAsync(flag + nh, 0, sizeof(uint32_t), s));
         tb = 0;
@@ -1379,9 +1399,9 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
         PGD_CUDA(ctx, cudaMemcpyAsync(&ni, fpos + nh, sizeof(ni), cudaMemcpyDeviceToHost, s));
         PGD_CUDA(ctx, cudaStreamSynchronize(s));
         nitems = ni;
-        if ((st = pgd_tmp_alloc(ctx, (void **)&items, (nitems + 1) * sizeof(int64_t)))) return st;
+        if ((st = tg.alloc(&items, (nitems + 1) * sizeof(int64_t)))) return st;
         PGD_LAUNCH(ctx, k_item_fill, grid_for(nh), kThreads, 0, flag, fpos, (int64_t)nh, items);
-        if ((st = pgd_tmp_alloc(ctx, (void **)&hrec, (nh + 1) * sizeof(int2)))) return st;
+        if ((st = tg.alloc(&hrec, (nh + 1) * sizeof(int2)))) return st;
         PGD_LAUNCH(ctx, k_hub_recs, grid_for(nh), kThreads, 0, G, posv, (int64_t)nh, hrec);
     }
     const int nsm = ctx->num_sms;
@@ -1393,7 +1413,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     if (sampled) PGD_LAUNCH(ctx, k_tslot, grid_for(32 * G.m), kThreads, 0, G, slot, nullptr, 0);
     if (nitems > 0) {
         if ((int64_t)H.split < G.n) {
-            if ((st = pgd_tmp_alloc(ctx, (void **)&gbm, (size_t)nsm * H.nwords * 4))) return st;
+            if ((st = tg.alloc(&gbm, (size_t)nsm * H.nwords * 4))) return st;
             PGD_CUDA(ctx, cudaMemsetAsync(gbm, 0, (size_t)nsm * H.nwords * 4, s));
         }
         HubArgs T = H;
@@ -1416,9 +1436,9 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
         PGD_LAUNCH(ctx, k_tslot, grid_for(32 * nlight), kThreads, 0, G, slot, posv + nh + nd, nlight);
     if (nitems > 0) {
         if (!H.smem_hist) {
-            if ((st = pgd_tmp_alloc(ctx, (void **)&ghist, (size_t)nsm * H.hstride * 4))) return st;
+            if ((st = tg.alloc(&ghist, (size_t)nsm * H.hstride * 4))) return st;
         }
-        if ((st = pgd_tmp_alloc(ctx, (void **)&thigh, (size_t)nsm * kHubWarps * kTHigh * sizeof(int32_t)))) return st;
+        if ((st = tg.alloc(&thigh, (size_t)nsm * kHubWarps * kTHigh * sizeof(int32_t)))) return st;
         PGD_CUDA(ctx, cudaFuncSetAttribute(k_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         H.G = G;
         H.hpos = posv;
@@ -1460,17 +1480,6 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     }
     PGD_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
     PGD_CUDA(ctx, cudaGetLastError());
-    pgd_tmp_free(ctx, keys);
-    pgd_tmp_free(ctx, keys2);
-    pgd_tmp_free(ctx, posv);
-    pgd_tmp_free(ctx, vals);
-    pgd_tmp_free(ctx, flag);
-    pgd_tmp_free(ctx, fpos);
-    pgd_tmp_free(ctx, items);
-    pgd_tmp_free(ctx, ghist);
-    pgd_tmp_free(ctx, gbm);
-    pgd_tmp_free(ctx, hrec);
-    pgd_tmp_free(ctx, thigh);
     PGD_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
     PGD_CUDA(ctx, cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
     return PGD_OK;
