@@ -104,6 +104,16 @@ struct DevGraph {
     int anchor_hub;             // anchors of degree >= this take the bitmap path
 };
 
+// Graph of a union id: last g in [0, k) with base[g] <= x (base non-decreasing).
+__device__ __forceinline__ int batch_find(const int64_t *base, int k, int64_t x) {
+    int lo = 0, hi = k;  // last g with base[g] <= x
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (base[mid] <= x) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
 __device__ __forceinline__ bool dense_edge(const DevGraph &G, int64_t e) {
     return G.gdense && G.gdense[G.egraph[e]];
 }
@@ -1051,13 +1061,21 @@ __device__ __forceinline__ int32_t dense_q(const DevGraph &G, int64_t e) {
 }
 
 // Sort keys grouping the dense-graph edges by q (then by position), so that
-// k_dense can serve several edges with one pass over A_q's rows.
-__global__ void k_dense_keys(DevGraph G, const int32_t *dpos, int64_t nd, uint64_t *keys, int32_t *vals) {
+// k_dense can serve several edges with one pass over A_q's rows.  Edges of
+// graphs with a common-neighbour matrix (cbase[g] >= 0) sort first: bit 63
+// is free because q < 2^31.
+__global__ void k_dense_keys(DevGraph G, const int32_t *dpos, int64_t nd, const int64_t *cbase, uint64_t *keys,
+                             int32_t *vals, unsigned long long *ncn) {
+    unsigned long long cnt = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t e = dpos[i];
-        keys[i] = ((uint64_t)(uint32_t)dense_q(G, e) << 32) | (uint32_t)e;
+        const uint64_t plain = (cbase && cbase[G.egraph[e]] >= 0) ? 0ull : 1ull;
+        keys[i] = (plain << 63) | ((uint64_t)(uint32_t)dense_q(G, e) << 32) | (uint32_t)e;
         vals[i] = e;
+        cnt += 1ull - plain;
     }
+    cnt = pgd_warp_sum(cnt);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(ncn, cnt);
 }
 
 constexpr int kDenseGroup = 6;   // edges sharing q decomposed together
@@ -1148,6 +1166,199 @@ __global__ void __launch_bounds__(256, 3) k_dense(DenseArgs A) {
                 const int64_t e = A.dpos[i0 + j];
                 const int32_t id = G.order[e];
                 edge_epilogue(G, acc, cur_g, e, G.ev[id], G.eu[id], t, k2 >> 1, c, lane);
+            }
+            i0 = i1;
+        }
+    }
+    block_flush(G, acc, cur_g, s_red, 8);
+}
+
+// ---------------------------------------------------------------------------
+// Dense graphs with a common-neighbour matrix.  For a graph of n vertices
+// (W = ceil(n/64) row words) CN[a][b] = |N(a) ∩ N(b)| = popc(A_a & A_b), in
+// 16-bit entries (n <= 2048), rows padded to 64·W entries so that a warp
+// reads 64 entries per row word.  With it, c4 of an edge (p, q) follows from
+//   c4 = sum_{w in S_q} CN[p][w] - |S_q| - sum_{x in T} CN[q][x] + 2·k4 + t
+// (for w in S_q, N(w) ∩ N(p) holds q, |N(w) ∩ T| members of T and the rest
+// of S_p; the edges between S_q and T number sum_{x in T} t(x, q) - 2·k4 - t,
+// t(x, q) = CN[q][x]), so only the rows of T's members are scanned (for k4),
+// not those of all of N(q).  Building CN costs n·64W·W word operations, which
+// pays off for graphs of average degree >= n/16.
+
+constexpr int kCnRows = 32;   // rows a of CN computed by one block
+
+// One block per tile of 32 rows a of one graph: the tile's bit rows in shared
+// memory, one column b per thread, 32 counters in registers.  ctile[g] is
+// the first tile of graph g (k + 1 entries, non-decreasing).
+__global__ void __launch_bounds__(256) k_dense_common(const uint64_t *bits, const int64_t *wbase,
+                                                      const long long *gnm, const int64_t *cbase,
+                                                      const int64_t *ctile, int k, int64_t ntiles, uint16_t *cn) {
+    __shared__ uint64_t sa[kCnRows][32];
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int g = batch_find(ctile, k, tile);
+        const int64_t n = gnm[2 * g];
+        const int W = (int)((n + 63) >> 6);
+        const int64_t stride = (int64_t)W * 64;
+        const int64_t a0 = (tile - ctile[g]) * kCnRows;
+        const uint64_t *rows = bits + wbase[g];
+        __syncthreads();   // the previous tile's rows are no longer read
+        for (int i = threadIdx.x; i < kCnRows * 32; i += blockDim.x) {
+            const int r = i >> 5, w = i & 31;
+            sa[r][w] = (a0 + r < n && w < W) ? rows[(a0 + r) * W + w] : 0ull;
+        }
+        __syncthreads();
+        uint16_t *out = cn + cbase[g];
+        for (int64_t b = threadIdx.x; b < stride; b += blockDim.x) {
+            uint32_t acc[kCnRows];
+#pragma unroll
+            for (int i = 0; i < kCnRows; i++) acc[i] = 0;
+            if (b < n) {
+                const uint64_t *rb = rows + b * W;
+                for (int w = 0; w < W; w++) {
+                    const uint64_t x = __ldg(rb + w);
+#pragma unroll
+                    for (int i = 0; i < kCnRows; i++) acc[i] += __popcll(x & sa[i][w]);
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < kCnRows; i++)
+                if (a0 + i < n) out[(a0 + i) * stride + b] = (uint16_t)acc[i];
+        }
+    }
+}
+
+struct DenseCnArgs {
+    DevGraph G;
+    const uint64_t *bits;
+    const int64_t *wbase;
+    const int64_t *vbase;
+    const uint16_t *cn;       // CN matrices of the graphs that have one
+    const int64_t *cbase;     // per graph: first entry of its CN matrix
+    const int32_t *dpos;      // E_ordered positions of those graphs' edges, grouped by q
+    int64_t ndense;
+    unsigned long long *next;
+};
+
+// Up to kDenseGroup edges (p_j, q) with the same q, as in k_dense; per row
+// word L of A_q the warp reads 64 entries of CN[q] and of each CN[p_j] (two
+// per lane) for the two sums, and the rows of the word's members of T_j.
+__global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
+    __shared__ unsigned long long s_red[8][PGD_NSUMS];
+    const DevGraph &G = A.G;
+    const int lane = threadIdx.x & 31;
+    int cur_g = -1;
+    unsigned long long acc[PGD_NSUMS];
+#pragma unroll
+    for (int i = 0; i < PGD_NSUMS; i++) acc[i] = 0;
+    while (true) {
+        unsigned long long idx = 0;
+        if (lane == 0) idx = atomicAdd(A.next, (unsigned long long)kDenseGroup);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if (idx >= (unsigned long long)A.ndense) break;
+        const int64_t iend = min(idx + (unsigned long long)kDenseGroup, (unsigned long long)A.ndense);
+        int64_t i0 = (int64_t)idx;
+        while (i0 < iend) {
+            const int32_t qg = dense_q(G, A.dpos[i0]);
+            int64_t i1 = i0 + 1;
+            while (i1 < iend && dense_q(G, A.dpos[i1]) == qg) i1++;
+            const int R = (int)(i1 - i0);
+            const int g = G.egraph[A.dpos[i0]];
+            const int64_t vb = A.vbase[g];
+            const int W = (int)((G.gnm[2 * g] + 63) >> 6);
+            const int64_t stride = (int64_t)W * 64;
+            const uint64_t *rows = A.bits + A.wbase[g];
+            const uint16_t *cnb = A.cn + A.cbase[g];
+            const int64_t q = qg - vb;
+            const uint16_t *cq = cnb + q * stride;
+            const uint64_t Aq = lane < W ? __ldg(rows + q * W + lane) : 0ull;
+            uint64_t T[kDenseGroup], Sq[kDenseGroup];
+            int32_t pl[kDenseGroup];
+            unsigned k4x2[kDenseGroup];
+            int dsum[kDenseGroup];   // this lane's share of sum_{S_q} CN[p][w] - sum_T CN[q][x]
+#pragma unroll
+            for (int j = 0; j < kDenseGroup; j++) {
+                T[j] = Sq[j] = 0;
+                pl[j] = 0;
+                k4x2[j] = 0;
+                dsum[j] = 0;
+                if (j < R) {
+                    const int32_t id = G.order[A.dpos[i0 + j]];
+                    const int32_t v = G.ev[id], u = G.eu[id];
+                    const int64_t p = (v == qg ? u : v) - vb;
+                    const uint64_t Ap = lane < W ? __ldg(rows + p * W + lane) : 0ull;
+                    const uint64_t bp = (lane == (int)(p >> 6)) ? (1ull << (p & 63)) : 0ull;
+                    T[j] = Ap & Aq;
+                    Sq[j] = Aq & ~Ap & ~bp;
+                    pl[j] = (int32_t)p;
+                }
+            }
+            for (int L = 0; L < W; L++) {
+                // word L of every T_j as 32-bit halves
+                uint32_t tlo[kDenseGroup], thi[kDenseGroup];
+                uint32_t ulo = 0, uhi = 0;
+#pragma unroll
+                for (int j = 0; j < kDenseGroup; j++) {
+                    tlo[j] = __shfl_sync(0xffffffffu, (uint32_t)T[j], L);
+                    thi[j] = __shfl_sync(0xffffffffu, (uint32_t)(T[j] >> 32), L);
+                    ulo |= tlo[j];
+                    uhi |= thi[j];
+                }
+                // entries 64L + 2·lane and the next of CN[q] and CN[p_j]; their
+                // bits are bits 2·lane, 2·lane + 1 of the word: of its low half
+                // for lanes 0-15, of its high half for lanes 16-31
+                const int64_t col = (int64_t)L * 64 + 2 * lane;
+                const uint32_t cq2 = __ldg((const uint32_t *)(cq + col));
+                const int sh = (2 * lane) & 31;
+#pragma unroll
+                for (int j = 0; j < kDenseGroup; j++) {
+                    const uint32_t slo = __shfl_sync(0xffffffffu, (uint32_t)Sq[j], L);
+                    const uint32_t shi = __shfl_sync(0xffffffffu, (uint32_t)(Sq[j] >> 32), L);
+                    if (j < R) {
+                        const uint32_t cp2 = __ldg((const uint32_t *)(cnb + (int64_t)pl[j] * stride + col));
+                        const unsigned sb = (lane < 16 ? slo : shi) >> sh, tb = (lane < 16 ? tlo[j] : thi[j]) >> sh;
+                        dsum[j] += (int)(((sb & 1u) ? (cp2 & 0xffffu) : 0u) + ((sb & 2u) ? (cp2 >> 16) : 0u)) -
+                                   (int)(((tb & 1u) ? (cq2 & 0xffffu) : 0u) + ((tb & 2u) ? (cq2 >> 16) : 0u));
+                    }
+                }
+                // rows of this word's members of the T_j (k4), one half at a
+                // time, two rows in flight, each row tested against every T_j
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    uint32_t u = h ? uhi : ulo;
+                    const uint64_t *rb = rows + ((int64_t)L * 64 + 32 * h) * W + lane;
+                    while (u) {
+                        const int b0 = __ffs(u) - 1;
+                        u &= u - 1;
+                        int b1 = -1;
+                        if (u) {
+                            b1 = __ffs(u) - 1;
+                            u &= u - 1;
+                        }
+                        const uint32_t m0 = 1u << b0, m1 = b1 >= 0 ? (1u << b1) : 0u;
+                        const uint64_t r0 = lane < W ? __ldg(rb + (int64_t)b0 * W) : 0ull;
+                        const uint64_t r1 = (b1 >= 0 && lane < W) ? __ldg(rb + (int64_t)b1 * W) : 0ull;
+#pragma unroll
+                        for (int j = 0; j < kDenseGroup; j++) {
+                            const uint32_t tj = h ? thi[j] : tlo[j];
+                            if (tj & m0) k4x2[j] += __popcll(r0 & T[j]);
+                            if (tj & m1) k4x2[j] += __popcll(r1 & T[j]);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < kDenseGroup; j++) {
+                if (j >= R) break;
+                const unsigned long long t = pgd_warp_sum(__popcll(T[j]));
+                const unsigned long long nsq = pgd_warp_sum(__popcll(Sq[j]));
+                const unsigned long long k4 = pgd_warp_sum(k4x2[j]) >> 1;
+                // sum_{S_q} CN[p][w] - sum_T CN[q][x]: lane shares are signed, the
+                // warp's total modulo 2^64 is exact (|total| < 2^23)
+                const unsigned long long dtot = pgd_warp_sum((unsigned long long)(long long)dsum[j]);
+                const unsigned long long c = dtot + 2 * k4 + t - nsq;
+                const int64_t e = A.dpos[i0 + j];
+                const int32_t id = G.order[e];
+                edge_epilogue(G, acc, cur_g, e, G.ev[id], G.eu[id], t, k4, c, lane);
             }
             i0 = i1;
         }
@@ -1327,6 +1538,8 @@ struct DenseView {
     const uint64_t *bits;
     const int64_t *wbase;
     const int64_t *vbase;
+    const uint16_t *cn;       // common-neighbour matrices (null: none)
+    const int64_t *cbase;     // per graph: first CN entry, or -1
 };
 
 // Where k_hub keeps the W histogram and the N(p) rank bitmap: the histogram
@@ -1453,22 +1666,46 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     }
     if (nd > 0 && dense) {
         // dense edges grouped by q, so that k_dense serves several per row pass
-        PGD_LAUNCH(ctx, k_dense_keys, grid_for(nd), kThreads, 0, G, posv + nh, (int64_t)nd, keys, vals);
+        // (edges of graphs with a CN matrix first, counted in ctr[7])
+        PGD_LAUNCH(ctx, k_dense_keys, grid_for(nd), kThreads, 0, G, posv + nh, (int64_t)nd,
+                   dense->cn ? dense->cbase : nullptr, keys, vals, ctr + 7);
         size_t tbd = 0;
         void *tmpd = nullptr;
         cub::DeviceRadixSort::SortPairs(nullptr, tbd, keys, keys2, vals, posv + nh, (int64_t)nd, 0, 64, s);
         if ((st = pgd_tmp_alloc(ctx, &tmpd, tbd))) return st;
         cub::DeviceRadixSort::SortPairs(tmpd, tbd, keys, keys2, vals, posv + nh, (int64_t)nd, 0, 64, s);
         pgd_tmp_free(ctx, tmpd);
-        DenseArgs D;
-        D.G = G;
-        D.bits = dense->bits;
-        D.wbase = dense->wbase;
-        D.vbase = dense->vbase;
-        D.dpos = posv + nh;
-        D.ndense = (int64_t)nd;
-        D.next = ctr + 4;
-        PGD_LAUNCH(ctx, k_dense, nsm * 8, 256, 0, D);
+        int64_t ncn = 0;
+        if (dense->cn) {
+            unsigned long long h = 0;
+            PGD_CUDA(ctx, cudaMemcpyAsync(&h, ctr + 7, sizeof(h), cudaMemcpyDeviceToHost, s));
+            PGD_CUDA(ctx, cudaStreamSynchronize(s));
+            ncn = (int64_t)h;
+        }
+        if (ncn > 0) {
+            DenseCnArgs C;
+            C.G = G;
+            C.bits = dense->bits;
+            C.wbase = dense->wbase;
+            C.vbase = dense->vbase;
+            C.cn = dense->cn;
+            C.cbase = dense->cbase;
+            C.dpos = posv + nh;
+            C.ndense = ncn;
+            C.next = ctr + 6;
+            PGD_LAUNCH(ctx, k_dense_cn, nsm * 8, 256, 0, C);
+        }
+        if ((int64_t)nd > ncn) {
+            DenseArgs D;
+            D.G = G;
+            D.bits = dense->bits;
+            D.wbase = dense->wbase;
+            D.vbase = dense->vbase;
+            D.dpos = posv + nh + ncn;
+            D.ndense = (int64_t)nd - ncn;
+            D.next = ctr + 4;
+            PGD_LAUNCH(ctx, k_dense, nsm * 8, 256, 0, D);
+        }
     }
     if (nlight > 0) {
         LightArgs L;
@@ -1524,15 +1761,6 @@ struct BatchDesc {
     int64_t n, m, vbase, ebase, sbase;   // vertex, edge and slot offsets in the union
 };
 
-__device__ __forceinline__ int batch_find(const int64_t *base, int k, int64_t x) {
-    int lo = 0, hi = k;  // last g with base[g] <= x
-    while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (base[mid] <= x) lo = mid; else hi = mid;
-    }
-    return lo;
-}
-
 __global__ void k_union_vertices(const BatchDesc *D, const int64_t *vbase, int k, int64_t N, int64_t *off,
                                  int32_t *deg, int32_t *vgraph) {
     for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < N; x += (int64_t)gridDim.x * blockDim.x) {
@@ -1561,6 +1789,32 @@ __global__ void k_union_edges(const BatchDesc *D, const int64_t *ebase, int k, i
         order[e] = (int32_t)(D[g].order[l] + D[g].ebase);
         egraph[e] = g;
     }
+}
+
+// Graphs of a batch that also get a common-neighbour matrix (k_dense_cn):
+// graphs on the row-bitset path whose average degree is at least n/16
+// (32·m >= n²), as long as the matrices stay within kCnMaxEntries.  Fills
+// cbase (first entry per graph, -1 for none) and ctile (first 32-row tile
+// per graph; k + 1 entries) and returns the number of 16-bit entries.
+constexpr int64_t kCnMaxEntries = 4ll << 30;   // 8 GiB
+
+static int64_t plan_common(int k, const std::vector<long long> &gnm, const std::vector<uint8_t> &gdense,
+                           std::vector<int64_t> &cbase, std::vector<int64_t> &ctile) {
+    cbase.assign((size_t)k, -1);
+    ctile.assign((size_t)k + 1, 0);
+    int64_t entries = 0, tiles = 0;
+    for (int g = 0; g < k; g++) {
+        ctile[(size_t)g] = tiles;
+        const int64_t n = gnm[(size_t)2 * g], m = gnm[(size_t)2 * g + 1];
+        if (!gdense[(size_t)g] || 32 * m < n * n) continue;
+        const int64_t e = n * (((n + 63) / 64) * 64);   // a multiple of 64: every matrix is 128-byte aligned
+        if (entries + e > kCnMaxEntries) continue;
+        cbase[(size_t)g] = entries;
+        entries += e;
+        tiles += (n + kCnRows - 1) / kCnRows;
+    }
+    ctile[(size_t)k] = tiles;
+    return entries;
 }
 
 pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k, bool micro, pgd_counts *out) {
@@ -1617,7 +1871,8 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
     unsigned long long *gsums = nullptr, *bits = nullptr;
     uint64_t *umicro = nullptr;
     uint8_t *d_gdense = nullptr;
-    int64_t *d_wbase = nullptr;
+    int64_t *d_wbase = nullptr, *d_cbase = nullptr, *d_ctile = nullptr;
+    uint16_t *cn = nullptr;
     // graphs of at most dense_max vertices use the row-bitset kernel
     std::vector<uint8_t> gdense((size_t)k, 0);
     std::vector<int64_t> wbase((size_t)k, 0);
@@ -1632,7 +1887,12 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
             ndense_graphs++;
         }
     }
+    std::vector<int64_t> cbase, ctile;
+    const int64_t cn_entries = plan_common(k, gnm, gdense, cbase, ctile);
     auto cleanup = [&]() {
+        pgd_tmp_free(ctx, cn);
+        pgd_tmp_free(ctx, d_cbase);
+        pgd_tmp_free(ctx, d_ctile);
         pgd_tmp_free(ctx, vgraph);
         pgd_tmp_free(ctx, bits);
         pgd_tmp_free(ctx, d_gdense);
@@ -1676,6 +1936,11 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
     BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&d_gdense, (size_t)k));
     BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&d_wbase, (size_t)k * sizeof(int64_t)));
     if (words > 0) BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&bits, (size_t)words * sizeof(unsigned long long)));
+    if (cn_entries > 0) {
+        BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&cn, (size_t)cn_entries * sizeof(uint16_t)));
+        BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&d_cbase, (size_t)k * sizeof(int64_t)));
+        BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&d_ctile, ((size_t)k + 1) * sizeof(int64_t)));
+    }
     BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&gsums, (size_t)k * PGD_NSUMS * sizeof(unsigned long long)));
     if (micro) BATCH_TRY(pgd_tmp_alloc(ctx, (void **)&umicro, (M + 1) * PGD_NMICRO * sizeof(uint64_t)));
     BATCH_TRY(pgd_graph_alloc(&U, (void **)&U.off, (N + 1) * sizeof(int64_t)));
@@ -1690,7 +1955,10 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
         cudaMemsetAsync(gsums, 0, (size_t)k * PGD_NSUMS * sizeof(unsigned long long), s) ||
         cudaMemcpyAsync(d_gdense, gdense.data(), (size_t)k, cudaMemcpyHostToDevice, s) ||
         cudaMemcpyAsync(d_wbase, wbase.data(), (size_t)k * sizeof(int64_t), cudaMemcpyHostToDevice, s) ||
-        (words > 0 && cudaMemsetAsync(bits, 0, (size_t)words * sizeof(unsigned long long), s))) {
+        (words > 0 && cudaMemsetAsync(bits, 0, (size_t)words * sizeof(unsigned long long), s)) ||
+        (cn_entries > 0 &&
+         (cudaMemcpyAsync(d_cbase, cbase.data(), (size_t)k * sizeof(int64_t), cudaMemcpyHostToDevice, s) ||
+          cudaMemcpyAsync(d_ctile, ctile.data(), ((size_t)k + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s)))) {
         cleanup();
         return pgd_fail(ctx, PGD_ECUDA, "batch set-up copy failed");
     }
@@ -1703,13 +1971,16 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
     if (words > 0)
         PGD_LAUNCH(ctx, k_dense_bits, grid_for(32 * N), kThreads, 0, U.off, U.adj, vgraph, d_gdense, d_wbase, d_bases,
                    d_gnm, N, bits);
+    if (cn_entries > 0)
+        PGD_LAUNCH(ctx, k_dense_common, (int)std::min<int64_t>(ctile[(size_t)k], (int64_t)ctx->num_sms * 8), 256, 0,
+                   (const uint64_t *)bits, d_wbase, d_gnm, d_cbase, d_ctile, k, ctile[(size_t)k], cn);
     DevGraph G = dev_view(&U, micro);
     G.micro = micro ? umicro : nullptr;
     G.sums = gsums;
     G.egraph = egraph;
     G.gnm = d_gnm;
     G.gdense = ndense_graphs ? d_gdense : nullptr;
-    DenseView dv{(const uint64_t *)bits, d_wbase, d_bases};
+    DenseView dv{(const uint64_t *)bits, d_wbase, d_bases, cn, d_cbase};
     float ms = 0;
     BATCH_TRY(run_decompose(ctx, G, (int4 *)U.slot, U.nhubs, U.max_degree, &ms, ndense_graphs ? &dv : nullptr));
     std::vector<unsigned long long> h((size_t)k * PGD_NSUMS);
@@ -2068,13 +2339,29 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
 
 namespace {
 
+// Largest vertex id of each graph's pairs (self loops excluded).  The warp
+// walks 32 consecutive pairs at a time; when they belong to one graph (the
+// usual case) it reduces them first and issues one atomic.
 __global__ void k_pairs_graph_max(const int64_t *pair_off, int k, const int32_t *src, const int32_t *dst, int64_t P,
                                   int *gmax, unsigned long long *bad) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P; i += (int64_t)gridDim.x * blockDim.x) {
-        const int g = batch_find(pair_off, k, i);
-        const int32_t a = src[i], b = dst[i];
-        if (a < 0 || b < 0) atomicAdd(bad, 1ull);
-        else if (a != b) atomicMax(gmax + g, max(a, b));
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < P; base += stride) {
+        const int64_t i = base + lane;
+        int g = -1, v = -1;
+        if (i < P) {
+            g = batch_find(pair_off, k, i);
+            const int32_t a = src[i], b = dst[i];
+            if (a < 0 || b < 0) atomicAdd(bad, 1ull);
+            else if (a != b) v = max(a, b);
+        }
+        const int g0 = __shfl_sync(0xffffffffu, g, 0);   // lane 0's pair is in range: base < P
+        if (__all_sync(0xffffffffu, g == g0 || g < 0)) {
+            const int wmax = __reduce_max_sync(0xffffffffu, v);
+            if (lane == 0 && wmax >= 0) atomicMax(gmax + g0, wmax);
+        } else if (v >= 0) {
+            atomicMax(gmax + g, v);
+        }
     }
 }
 
@@ -2115,6 +2402,8 @@ pgd_status pgd_dev_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pai
     const int64_t P1 = P > 0 ? P : 1;
     int32_t *d_src = nullptr, *d_dst = nullptr, *vgraph = nullptr, *egraph = nullptr, *row = nullptr;
     int64_t *d_poff = nullptr, *d_vbase = nullptr, *d_goff = nullptr, *d_wbase = nullptr;
+    int64_t *d_cbase = nullptr, *d_ctile = nullptr;
+    uint16_t *cn = nullptr;
     int *gmax = nullptr;
     uint32_t *flag = nullptr, *pos = nullptr;
     unsigned long long *gsums = nullptr, *bits = nullptr;
@@ -2125,7 +2414,8 @@ pgd_status pgd_dev_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pai
     auto cleanup = [&]() {
         for (void *p : {(void *)d_src, (void *)d_dst, (void *)vgraph, (void *)egraph, (void *)row, (void *)d_poff,
                         (void *)d_vbase, (void *)d_goff, (void *)d_wbase, (void *)gmax, (void *)flag, (void *)pos,
-                        (void *)gsums, (void *)bits, (void *)d_gnm, (void *)d_gdense})
+                        (void *)gsums, (void *)bits, (void *)d_gnm, (void *)d_gdense, (void *)cn, (void *)d_cbase,
+                        (void *)d_ctile})
             pgd_tmp_free(ctx, p);
         pgd_graph_destroy(U);
     };
@@ -2234,6 +2524,15 @@ pgd_status pgd_dev_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pai
             ndense_graphs++;
         }
     }
+    std::vector<int64_t> cbase, ctile;
+    const int64_t cn_entries = plan_common(k, gnm, gdense, cbase, ctile);
+    if (cn_entries > 0) {
+        PB_TRY(pgd_tmp_alloc(ctx, (void **)&cn, (size_t)cn_entries * sizeof(uint16_t)));
+        PB_TRY(pgd_tmp_alloc(ctx, (void **)&d_cbase, (size_t)k * sizeof(int64_t)));
+        PB_TRY(pgd_tmp_alloc(ctx, (void **)&d_ctile, ((size_t)k + 1) * sizeof(int64_t)));
+        PB_CUDA(cudaMemcpyAsync(d_cbase, cbase.data(), (size_t)k * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+        PB_CUDA(cudaMemcpyAsync(d_ctile, ctile.data(), ((size_t)k + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    }
     PB_TRY(pgd_tmp_alloc(ctx, (void **)&gsums, (size_t)k * PGD_NSUMS * sizeof(unsigned long long)));
     PB_TRY(pgd_tmp_alloc(ctx, (void **)&d_gnm, gnm.size() * sizeof(long long)));
     PB_TRY(pgd_tmp_alloc(ctx, (void **)&d_gdense, (size_t)k));
@@ -2250,12 +2549,15 @@ pgd_status pgd_dev_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pai
         if (words > 0)
             PGD_LAUNCH(ctx, k_dense_bits, grid_for(32 * N), kThreads, 0, U->off, U->adj, vgraph, d_gdense, d_wbase,
                        d_vbase, d_gnm, N, bits);
+        if (cn_entries > 0)
+            PGD_LAUNCH(ctx, k_dense_common, (int)std::min<int64_t>(ctile[(size_t)k], (int64_t)ctx->num_sms * 8), 256,
+                       0, (const uint64_t *)bits, d_wbase, d_gnm, d_cbase, d_ctile, k, ctile[(size_t)k], cn);
         DevGraph G = dev_view(U, false);
         G.sums = gsums;
         G.egraph = egraph;
         G.gnm = d_gnm;
         G.gdense = ndense_graphs ? d_gdense : nullptr;
-        DenseView dv{(const uint64_t *)bits, d_wbase, d_vbase};
+        DenseView dv{(const uint64_t *)bits, d_wbase, d_vbase, cn, d_cbase};
         PB_TRY(run_decompose(ctx, G, (int4 *)U->slot, U->nhubs, U->max_degree, &ms, ndense_graphs ? &dv : nullptr));
     }
     std::vector<unsigned long long> h((size_t)k * PGD_NSUMS);

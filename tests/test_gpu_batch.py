@@ -139,3 +139,43 @@ def test_hub_kernel_layouts(case):
     x, y, z = o.micro()
     assert (cols == z).all()
     c.close()
+
+
+def test_dense_graphs_common_neighbour_path():
+    """Batched graphs of at most 2048 vertices and average degree >= n/16 are
+    decomposed with a common-neighbour matrix (c4 from the identity over
+    CN[p][w] and CN[q][x]); sparser ones in the same batch keep the plain
+    row-bitset kernel.  Totals, raw sums and per-edge rows equal the
+    single-graph kernels' (k_hub / k_light), and the oracle's on the small
+    graphs."""
+    c = pgd.Context()
+    c.set_thresholds(128, 64, 2048)
+    specs = [(2048, 0.5), (2000, 0.07), (1500, 0.3), (1025, 0.2), (700, 0.9), (64, 1.0), (65, 0.5),
+             (300, 0.06), (129, 0.4), (33, 0.8), (1800, 0.01)]
+    pairs = [pgd.erdos_renyi(n, p, seed=100 + i) for i, (n, p) in enumerate(specs)]
+    pairs.append(pgd.barabasi_albert(900, 3, seed=8))
+    graphs = [c.graph_from_edges(s, d) for s, d in pairs]
+    cn_path = []
+    for g, (s, d) in zip(graphs, pairs):
+        g.preprocess("deg")
+        g.sort_edges("kcore")
+    res = c.decompose_batch(graphs, micro=True)
+    batch_rows = [g.micro() for g in graphs]
+    for i, (g, r) in enumerate(zip(graphs, res)):
+        cn_path.append(32 * r.m >= r.n * r.n)
+        single = g.decompose(micro=True)
+        assert (single.totals == r.totals).all(), i
+        assert (single.sums == r.sums).all(), i
+        a, b, cols = g.micro()
+        x, y, z = batch_rows[i]
+        assert (a == x).all() and (b == y).all() and (cols == z).all(), i
+    assert sum(cn_path) >= 7 and not all(cn_path)
+    for i in (5, 6, 8, 9, 7):
+        o = ol.OracleGraph.from_pairs(*pairs[i], dedup=True).run(order="kcore")
+        assert (res[i].totals == o.totals()).all(), i
+        assert (batch_rows[i][2] == o.micro()[2]).all(), i
+    # the pairs batch (device CSR build of the union) agrees
+    pr = c.decompose_pairs_batch(pairs)
+    for i, r in enumerate(pr):
+        assert (r.totals == res[i].totals).all(), i
+    c.close()
