@@ -266,3 +266,38 @@ def test_sampled_rows_equal_full_rows():
     assert len(c) == len(ids)
     for a, b, row in zip(s, d, c):
         assert (rows[(int(a), int(b))] == row).all()
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_c4_identity_used_by_the_kernels(seed):
+    """The decomposition kernels do not scan S_q x S_p for c4; they use
+      c4 = sum_{w in S_q} W(w,p) - |S_q| - sum_{x in T} t(x,q) + 2*k4 + t,
+    W(a,b) = |N(a) & N(b)|, t(x,q) = W(x,q) for x in T (k_hub reads W from a
+    histogram, k_dense_cn from a common-neighbour matrix).  The identity must
+    reproduce the oracle's per-edge c4 (the reference's S_u x S_v count) for
+    either choice of p and q, next to its t and k4."""
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(40, 160))
+    p_edge = float(rng.uniform(0.05, 0.6))
+    iu, ju = np.triu_indices(n, 1)
+    keep = rng.random(len(iu)) < p_edge
+    src, dst = iu[keep].astype(np.int32), ju[keep].astype(np.int32)
+    og = ol.OracleGraph.from_pairs(src, dst, dedup=True)
+    og.run(order="deg", micro=True)
+    s1, d1, cols = og.micro()
+    off, adj = og.csr()
+    nn = len(off) - 1
+    A = np.zeros((nn, nn), bool)
+    for v in range(nn):
+        A[v, adj[off[v]:off[v + 1]]] = True
+    W = A.astype(np.int64) @ A.astype(np.int64)
+    assert len(cols) == og.m > 0
+    for (a, b), row in zip(zip(s1 - 1, d1 - 1), cols):
+        t, k4, c4 = int(row[0]), int(row[2]), int(row[5])
+        T = A[a] & A[b]
+        assert T.sum() == t and W[a, b] == t
+        for p, q in ((a, b), (b, a)):
+            Sq = A[q] & ~A[p]
+            Sq[p] = False
+            got = int(W[Sq, p].sum()) - int(Sq.sum()) - int(W[T, q].sum()) + 2 * k4 + t
+            assert got == c4, (p, q, got, c4)
