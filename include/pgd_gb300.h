@@ -273,7 +273,9 @@ pgd_status pgd_server_destroy(pgd_server *sv);
  * it, below it N(w) is scanned per edge.  dense_max (0..2048, default 2048): in a batch,
  * graphs of at most this many vertices are decomposed with whole adjacency
  * rows as bitsets (one 2048-bit row per warp), larger ones with sorted
- * lists.  pgd_autotune decomposes the given graphs `reps` times per
+ * lists; those of average degree >= n/16 also get a 16-bit common-neighbour
+ * matrix (about 2·n² bytes of device memory while the batch runs).
+ * pgd_autotune decomposes the given graphs `reps` times per
  * candidate -- first dense_max in {0, 256, 1024, 2048}, then 16
  * (anchor_hub, cache_hub) pairs -- checks that every candidate gives
  * identical counts, keeps the fastest on the context and reports it. */
