@@ -35,9 +35,14 @@ METRIC = "edges/s full 4-node counts (bit-exact)"
 UNIT = "edges/s"
 RMAT = dict(a=0.57, b=0.19, c=0.19)
 
-# DRAM traffic (read + write) of one k_hub launch, the dominant kernel, on
-# this workload: a full-size single-pass ncu capture, profiles/k_hub_rmat20_dram.md.
-NCU_TRAFFIC_BYTES = 386210242048 + 1407233792
+# ncu figures of one k_hub launch (the dominant kernel) on this workload, read
+# from the committed summary: a `bench-figures:` line holding JSON with the
+# DRAM traffic, the L2 request bytes, issue activity and the SHA-256 of the
+# decompose.cu the capture ran.  A summary whose source hash differs from
+# the current file is reported as stale.
+PROFILE = os.path.join(ROOT, "profiles", "k_hub_rmat20_dram.md")
+KERNEL_SRC = os.path.join(ROOT, "pgd_gb300", "csrc", "decompose.cu")
+GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
 def log(*a):
@@ -115,14 +120,47 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def algorithmic_bytes(ev, eu, n, micro=True):
+def algorithmic_bytes(ev, eu, n, micro=True, anchor_hub=None):
     """Bytes an edge-centric decomposition must stream: per edge both
     endpoint lists plus the 2-hop lists of the cheaper endpoint, 4 B per
-    adjacency entry, plus 64 B of per-edge output (micro)."""
+    adjacency entry, plus 64 B of per-edge output (micro).  With anchor_hub,
+    only the edges whose anchor (the endpoint of higher (degree, id)) has at
+    least that degree: the units of the hub-anchored kernel.  Returns
+    (bytes, edges counted)."""
     deg = np.bincount(ev, minlength=n) + np.bincount(eu, minlength=n)
     vol2 = np.bincount(ev, weights=deg[eu], minlength=n) + np.bincount(eu, weights=deg[ev], minlength=n)
-    entries = (deg[ev] + deg[eu]).sum(dtype=np.float64) + np.minimum(vol2[ev], vol2[eu]).sum(dtype=np.float64)
-    return 4.0 * entries + (64.0 * len(ev) if micro else 0.0)
+    sel = slice(None)
+    if anchor_hub is not None:
+        dv, du = deg[ev], deg[eu]
+        dp = np.where((dv > du) | ((dv == du) & (ev > eu)), dv, du)
+        sel = dp >= anchor_hub
+    a, b = ev[sel], eu[sel]
+    entries = (deg[a] + deg[b]).sum(dtype=np.float64) + np.minimum(vol2[a], vol2[b]).sum(dtype=np.float64)
+    return 4.0 * entries + (64.0 * len(a) if micro else 0.0), int(len(a))
+
+
+def profile_figures():
+    """The bench-figures JSON of the committed k_hub summary, with whether it
+    was taken on the current kernel source."""
+    import hashlib
+
+    out = {}
+    if os.path.exists(PROFILE):
+        for line in open(PROFILE):
+            if line.startswith("bench-figures:"):
+                out = json.loads(line.split(":", 1)[1])
+    src = hashlib.sha256(open(KERNEL_SRC, "rb").read()).hexdigest()
+    out["current_source"] = out.get("source_sha256") == src
+    return out
+
+
+def golden_totals(scale, order):
+    """The oracle's full-run totals of this workload, where committed."""
+    p = os.path.join(GOLDEN, "rmat%d_%s.json" % (scale, order))
+    if not os.path.exists(p):
+        return None
+    g = json.load(open(p))
+    return g
 
 
 def cpu_sample(src, dst, order, target_s, threads):
@@ -134,7 +172,7 @@ def cpu_sample(src, dst, order, target_s, threads):
     import oracle_lib as ol
 
     og = ol.OracleGraph.from_pairs(src, dst, dedup=True)
-    m = og.m
+    n, m = og.n, og.m
     kind = "port"
     runner = None
     if ol.ref_available():
@@ -159,23 +197,28 @@ def cpu_sample(src, dst, order, target_s, threads):
     while sec < target_s / 4 and stride > 1:
         stride = max(1, int(stride * max(sec, 1e-3) / target_s))
         k, sec = runner(stride)
-    return kind, k, sec, stride, m
+    return kind, k, sec, stride, n, m
 
 
 def run_reference_arm(args):
+    """The reference's per-edge loop on the host cores (oracle/_ref where the
+    reference was compiled, else the oracle's port of it).  The input comes
+    from the oracle's own RMAT generator, so this arm never loads the
+    product library."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import pgd_gb300 as pgd
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as ol
 
     threads = os.cpu_count() or 1
-    src, dst = pgd.rmat(args.scale, 16, seed=1, **RMAT)
+    src, dst = ol.rmat(args.scale, 16, seed=1, **RMAT)
     target = args.cpu_seconds
     per = []
     kind = None
     total_e, total_s = 0, 0.0
     for step in range(args.warmup + args.steps):
-        kind, k, sec, stride, m = cpu_sample(src, dst, args.order, target, threads)
+        kind, k, sec, stride, n, m = cpu_sample(src, dst, args.order, target, threads)
         if step >= args.warmup:
             total_e += k
             total_s += sec
@@ -186,7 +229,7 @@ def run_reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / max(1, args.steps),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-        "data": "synthetic (seeded RMAT generator)", "config": workload_config(args.scale, args.order),
+        "data": "synthetic (seeded RMAT generator)", "config": workload_config(args.scale, args.order, n, m),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -201,7 +244,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=int, default=20)
     ap.add_argument("--order", default="kcore")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -265,13 +308,20 @@ def main():
         log("rank %d: warmup %d kernel %.1f ms" % (rank, w, r.kernel_ms))
         if ref_totals is None:
             ref_totals = r.totals.copy()
+            gold = golden_totals(args.scale, args.order)
+            if gold is not None:
+                got = {k_: int(v) for k_, v in zip(pgd.TOTAL_NAMES, r.totals)}
+                if got != gold["totals"] or [int(x) for x in r.sums] != gold["sums"] or (n, m) != (gold["n"], gold["m"]):
+                    raise SystemExit("the decomposition differs from the oracle's full run "
+                                     "(tests/golden/rmat%d_%s.json): %s" % (args.scale, args.order, got))
+                log("rank %d: totals and raw sums equal the oracle's full run" % rank)
         assert (r.totals == ref_totals).all(), "decomposition not repeatable"
 
     # ---- timed region ------------------------------------------------------
     clocks = ClockSampler(local)
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
-    kernel_ms = []
+    kernel_ms, hub_ms = [], []
     launches0 = ctx.kernel_launches
     clocks.start()
     barrier()
@@ -282,6 +332,7 @@ def main():
             flush.zero_()
         r = step()
         kernel_ms.append(r.kernel_ms)
+        hub_ms.append(r.hub_ms)
         if ref_totals is not None:
             assert (r.totals == ref_totals).all(), "decomposition not repeatable"
     ev1.record(stream)
@@ -292,19 +343,36 @@ def main():
     window_ms = max_over_ranks(ev0.elapsed_time(ev1))
     value = world * m * args.steps / (window_ms / 1000.0)
     ms_per_step = window_ms / args.steps
-    log("rank %d: %.1f ms/step, kernel %.1f ms, %.3g edges/s" % (rank, ms_per_step, np.mean(kernel_ms), value))
+    log("rank %d: %.1f ms/step, decomposition kernels %.1f ms (k_hub %.1f ms), %.3g edges/s"
+        % (rank, ms_per_step, np.mean(kernel_ms), np.mean(hub_ms), value))
 
-    # ---- roofline of the decomposition kernel -----------------------------
+    # ---- roofline of the dominant kernel (k_hub) ----------------------------
+    # achieved = the per-edge algorithmic bytes of the edges k_hub decomposes
+    # (hub-anchored edges) over k_hub's own mean duration (CUDA events on the
+    # launching stream); traffic, L2 bytes and issue activity come from the
+    # committed ncu summary of the same launch on this workload.
     ev, eu, _ = g.edges(with_order=False)
-    b_alg = algorithmic_bytes(ev, eu, n, micro=True)
-    kern_s = float(np.mean(kernel_ms)) / 1000.0
+    anchor_hub = ctx.thresholds()[0]
+    b_alg, units = algorithmic_bytes(ev, eu, n, micro=True, anchor_hub=anchor_hub)
+    hub_s = float(np.mean(hub_ms)) / 1000.0
     peak, peak_src = peaks()
-    achieved = b_alg / kern_s / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": NCU_TRAFFIC_BYTES if args.scale == 20 and args.order == "kcore" else None,
-                "kernel": "k_hub (91 % of the device time in the ncu launch list)", "kernel_ms": float(np.mean(kernel_ms)),
-                "algorithmic_bytes": b_alg, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)"
-                if peak_src == "measured" else "fallback 6.8 TB/s"}
+    achieved = b_alg / hub_s / 1e9
+    prof = profile_figures() if (args.scale, args.order) == (20, "kcore") else {}
+    traffic = prof.get("traffic_bytes")
+    l2_bytes = prof.get("l2_bytes")
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+        "traffic": traffic, "kernel": "k_hub", "kernel_ms": 1000.0 * hub_s, "units": units,
+        "unit_name": "hub-anchored edges (anchor degree >= %d)" % anchor_hub,
+        "algorithmic_bytes": b_alg,
+        "dram_frac": (traffic / hub_s / 1e9 / peak) if traffic else None,
+        "model_bytes": l2_bytes,
+        "frac_model": (l2_bytes / hub_s / 1e9 / peak) if l2_bytes else None,
+        "issue_active": prof.get("issue_active"),
+        "profile_on_current_source": prof.get("current_source"),
+        "decomposition_kernels_ms": float(np.mean(kernel_ms)),
+        "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else "fallback 6.8 TB/s",
+    }
 
     # ---- end to end through the public API --------------------------------
     e2e = None
@@ -349,7 +417,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        kind, k, sec, stride, _ = cpu_sample(src, dst, args.order, args.cpu_seconds, threads)
+        kind, k, sec, stride, _, _ = cpu_sample(src, dst, args.order, args.cpu_seconds, threads)
         cpu = {"value": k / sec, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": "every %d-th edge of the %s order: %d of %d edges, global counts, %.1f s" %
                          (stride, args.order, k, m, sec)}

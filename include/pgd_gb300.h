@@ -74,7 +74,9 @@ typedef struct {
     int64_t n;              /* vertices                                     */
     int64_t m;              /* undirected edges                             */
     float kernel_ms;        /* device time of the decomposition kernels     */
-    float reserved[3];
+    float hub_ms;           /* of which the hub-anchored kernel (k_hub)     */
+    float tri_ms;           /* of which the triangle pass (t of every edge) */
+    float reserved;
 } pgd_counts;
 
 /* Graph summary (graphlet_core::basic_stats, graphlet_core.cpp:562-568). */

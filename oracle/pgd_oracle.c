@@ -661,6 +661,23 @@ static inline void edge_sums(ull *s, long long dv, long long du, ull t, long lon
     s[14] += t * disc;                            /* N10 */
 }
 
+/* Micro stores (graphlet_core.cpp:1559-1575) and the 2-star column of the
+ * writer (graphlet_core.h:353-355): the 8 per-edge columns of an edge from
+ * its endpoint degrees and t, k4, c4. */
+void po_micro_row(long long dv, long long du, uint64_t t, uint64_t k4, uint64_t c4, uint64_t row[PO_NMICRO]) {
+    long long sv = dv - (long long)t - 1, su = du - (long long)t - 1;
+    ull star3 = (ull)((double)(sv * (sv - 1)) * 0.5);
+    star3 = (ull)((double)star3 + (double)(su * (su - 1)) * 0.5);
+    row[0] = t;
+    row[1] = ((ull)dv - t) + ((ull)du - t) - 2;
+    row[2] = k4;
+    row[3] = (ull)((double)(t * (t - 1)) * 0.5 - (double)k4);
+    row[4] = 0; /* local_4_tailed_tris is never written (:1501) */
+    row[5] = c4;
+    row[6] = star3 - 0;
+    row[7] = (ull)(sv * su) - c4;
+}
+
 /* Closing identities (graphlet_core.cpp:1449-1472) and compute_4indep
  * (graphlet_core.h:548-557).  The reference is built with -ffast-math, under
  * which g++ turns x/3.0 and x/6.0 into multiplications by the rounded
@@ -767,22 +784,7 @@ int po_decompose(po_graph *g, int micro, int threads, int cheap_side) {
             loc[3] += k4;
             loc[4] += c4;
             g->t_e[id] = t; g->k4_e[id] = k4; g->c4_e[id] = c4;
-            if (micro) {
-                /* micro stores (graphlet_core.cpp:1559-1575) and the 2-star
-                 * column of the writer (graphlet_core.h:353-355) */
-                ull *row = (ull *)(g->micro + (size_t)e * PO_NMICRO);
-                long long sv = dv - (long long)t - 1, su = du - (long long)t - 1;
-                ull star3 = (ull)((double)(sv * (sv - 1)) * 0.5);
-                star3 = (ull)((double)star3 + (double)(su * (su - 1)) * 0.5);
-                row[0] = t;
-                row[1] = ((ull)dv - t) + ((ull)du - t) - 2;
-                row[2] = k4;
-                row[3] = (ull)((double)(t * (t - 1)) * 0.5 - (double)k4);
-                row[4] = 0; /* local_4_tailed_tris is never written (:1501) */
-                row[5] = c4;
-                row[6] = star3 - 0;
-                row[7] = (ull)(sv * su) - c4;
-            }
+            if (micro) po_micro_row(dv, du, t, k4, c4, g->micro + (size_t)e * PO_NMICRO);
         }
 #pragma omp critical
         for (int k = 0; k < PO_NSUMS; k++) total[k] += loc[k];
@@ -929,4 +931,41 @@ void po_get_edge_tkc(const po_graph *g, uint64_t *t, uint64_t *k4, uint64_t *c4)
     memcpy(t, g->t_e, (size_t)g->n_e * sizeof(uint64_t));
     memcpy(k4, g->k4_e, (size_t)g->n_e * sizeof(uint64_t));
     memcpy(c4, g->c4_e, (size_t)g->n_e * sizeof(uint64_t));
+}
+
+/* ------------------------------------------------------------------------ */
+/* Seeded RMAT input, restated independently of the product library so that
+ * the CPU baseline and the fixture scripts can make the benchmark's graph
+ * without loading it.  Draw l of edge i is u01(seed, "RMAT", i*scale + l),
+ * where u01 is the top 53 bits of the SplitMix64 output function (Steele,
+ * Lea, Flood, OOPSLA 2014) applied to a key and a counter; level l picks a
+ * quadrant with probabilities a, b, c, 1-a-b-c (b sets bit l of dst, c bit l
+ * of src, d both).  tests/test_oracle.py checks it against the product's
+ * generator pair for pair. */
+static uint64_t sm64(uint64_t x) {
+    x += 0x9e3779b97f4a7c15ull;
+    x ^= x >> 30; x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27; x *= 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+void po_gen_rmat(int scale, int edge_factor, double a, double b, double c, uint64_t seed, int32_t *src,
+                 int32_t *dst) {
+    const uint64_t key = sm64(seed ^ sm64(0x524d4154ull));   /* stream "RMAT" */
+    const int64_t draws = (int64_t)edge_factor << scale;
+    const double lim_a = a, lim_b = a + b, lim_c = a + b + c;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < draws; i++) {
+        uint32_t row = 0, col = 0;
+        uint64_t ctr = (uint64_t)i * (uint64_t)scale;
+        for (int l = 0; l < scale; l++, ctr++) {
+            double r = (double)(sm64(key + ctr) >> 11) / 9007199254740992.0;
+            uint32_t bit = 1u << l;
+            if (r >= lim_c) { row |= bit; col |= bit; }
+            else if (r >= lim_b) row |= bit;
+            else if (r >= lim_a) col |= bit;
+        }
+        src[i] = (int32_t)row;
+        dst[i] = (int32_t)col;
+    }
 }

@@ -70,6 +70,10 @@ int64_t po_decompose_sample(po_graph *g, int threads, int cheap_side, int64_t st
 int po_edge_sample(po_graph *g, int64_t k, const int64_t *vs, const int64_t *us, uint64_t *t, uint64_t *k4,
                    uint64_t *c4, int threads);
 
+/* The 8 per-edge columns of one edge (graphlet_core.cpp:1559-1575 and
+ * graphlet_core.h:353-355) from its endpoint degrees and t, k4, c4. */
+void po_micro_row(long long dv, long long du, uint64_t t, uint64_t k4, uint64_t c4, uint64_t row[PO_NMICRO]);
+
 /* Closing identities (graphlet_core.cpp:1449-1472, graphlet_core.h:548-557). */
 void po_close(const uint64_t sums[PO_NSUMS], int64_t n, int64_t m, uint64_t totals[PO_NTOTALS]);
 
@@ -90,6 +94,11 @@ void po_get_micro(const po_graph *g, int64_t *src1, int64_t *dst1, uint64_t *col
 /* Per-edge values by edge id (undirected edge index of e_v/e_u):
  * t, k4, c4 -- convenient for keyed comparisons. */
 void po_get_edge_tkc(const po_graph *g, uint64_t *t, uint64_t *k4, uint64_t *c4);
+
+/* Seeded RMAT pairs (edge_factor << scale draws), identical to the product's
+ * generator for the same arguments; src/dst hold edge_factor << scale ids. */
+void po_gen_rmat(int scale, int edge_factor, double a, double b, double c, uint64_t seed, int32_t *src,
+                 int32_t *dst);
 
 #ifdef __cplusplus
 }

@@ -66,7 +66,7 @@ class pgd_opts(ctypes.Structure):
 class pgd_counts(ctypes.Structure):
     _fields_ = [("totals", ctypes.c_uint64 * NTOTALS), ("sums", ctypes.c_uint64 * NSUMS),
                 ("n", ctypes.c_int64), ("m", ctypes.c_int64), ("kernel_ms", ctypes.c_float),
-                ("reserved", ctypes.c_float * 3)]
+                ("hub_ms", ctypes.c_float), ("tri_ms", ctypes.c_float), ("reserved", ctypes.c_float)]
 
 
 class pgd_server_opts(ctypes.Structure):
@@ -186,6 +186,7 @@ class Counts:
         self.totals = np.array(list(c.totals), dtype=np.uint64)
         self.sums = np.array(list(c.sums), dtype=np.uint64)
         self.n, self.m, self.kernel_ms = c.n, c.m, c.kernel_ms
+        self.hub_ms, self.tri_ms = c.hub_ms, c.tri_ms
 
     def as_dict(self):
         return {k: int(v) for k, v in zip(TOTAL_NAMES, self.totals)}

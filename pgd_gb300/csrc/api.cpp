@@ -110,7 +110,9 @@ extern "C" pgd_status pgd_context_create(const pgd_opts *opts, pgd_ctx **out) {
     }
     if (cudaMalloc((void **)&ctx->d_sums, 64 * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc((void **)&ctx->d_ctr, 64 * sizeof(unsigned long long)) != cudaSuccess ||
-        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+        cudaEventCreate(&ctx->evt0) != cudaSuccess || cudaEventCreate(&ctx->evt1) != cudaSuccess ||
+        cudaEventCreate(&ctx->evh0) != cudaSuccess || cudaEventCreate(&ctx->evh1) != cudaSuccess) {
         cudaGetLastError();
         pgd_context_destroy(ctx);
         return PGD_ECUDA;
@@ -127,6 +129,8 @@ extern "C" pgd_status pgd_context_destroy(pgd_ctx *ctx) {
     if (ctx->d_ctr) cudaFree(ctx->d_ctr);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    for (cudaEvent_t e : {ctx->evt0, ctx->evt1, ctx->evh0, ctx->evh1})
+        if (e) cudaEventDestroy(e);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return PGD_OK;

@@ -1559,12 +1559,17 @@ static size_t hub_layout(int64_t n, int32_t nhubs, int32_t max_degree, HubArgs *
     return (size_t)((H->smem_hist ? H->hstride : 0) + bm_words) * 4;
 }
 
+// Device times of one decomposition: all kernels, the triangle pass, k_hub.
+struct StageMs {
+    float total = 0, tri = 0, hub = 0;
+};
+
 static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int32_t nhubs, int32_t max_degree,
-                                float *ms, const DenseView *dense = nullptr) {
+                                StageMs *ms, const DenseView *dense = nullptr) {
     cudaStream_t s = ctx->stream;
     pgd_status st;
     const int64_t m = G.npos;   // positions to decompose (E_ordered length)
-    *ms = 0;
+    *ms = StageMs();
     if (m == 0) return PGD_OK;
     // a sampled order decomposes some edges but reads t(x, q) of any edge
     const bool sampled = G.npos < G.m;
@@ -1623,6 +1628,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     // (dense-graph edges need none).
     HubArgs H;
     const size_t smem = hub_layout(G.n, nhubs, max_degree, &H);
+    PGD_CUDA(ctx, cudaEventRecord(ctx->evt0, s));
     if (sampled) PGD_LAUNCH(ctx, k_tslot, grid_for(32 * G.m), kThreads, 0, G, slot, nullptr, 0);
     if (nitems > 0) {
         if ((int64_t)H.split < G.n) {
@@ -1647,6 +1653,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     }
     if (nlight > 0 && !sampled)
         PGD_LAUNCH(ctx, k_tslot, grid_for(32 * nlight), kThreads, 0, G, slot, posv + nh + nd, nlight);
+    PGD_CUDA(ctx, cudaEventRecord(ctx->evt1, s));
     if (nitems > 0) {
         if (!H.smem_hist) {
             if ((st = tg.alloc(&ghist, (size_t)nsm * H.hstride * 4))) return st;
@@ -1662,7 +1669,9 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
         H.gbitmap = gbm;
         H.next = ctr + 1;
         H.thigh = thigh;
+        PGD_CUDA(ctx, cudaEventRecord(ctx->evh0, s));
         PGD_LAUNCH(ctx, k_hub, nsm, kHubWarps * 32, smem, H);
+        PGD_CUDA(ctx, cudaEventRecord(ctx->evh1, s));
     }
     if (nd > 0 && dense) {
         // dense edges grouped by q, so that k_dense serves several per row pass
@@ -1718,7 +1727,9 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     PGD_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
     PGD_CUDA(ctx, cudaGetLastError());
     PGD_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
-    PGD_CUDA(ctx, cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
+    PGD_CUDA(ctx, cudaEventElapsedTime(&ms->total, ctx->ev0, ctx->ev1));
+    PGD_CUDA(ctx, cudaEventElapsedTime(&ms->tri, ctx->evt0, ctx->evt1));
+    if (nitems > 0) PGD_CUDA(ctx, cudaEventElapsedTime(&ms->hub, ctx->evh0, ctx->evh1));
     return PGD_OK;
 }
 
@@ -1731,7 +1742,7 @@ pgd_status pgd_dev_decompose(pgd_graph *g, bool micro, pgd_counts *out) {
     }
     if ((!g->has_aux || g->aux_cache_hub != ctx->cache_hub) && (st = build_aux(g))) return st;
     PGD_CUDA(ctx, cudaMemsetAsync(ctx->d_sums, 0, PGD_NSUMS * sizeof(unsigned long long), s));
-    float ms = 0;
+    StageMs ms;
     if ((st = run_decompose(ctx, dev_view(g, micro), (int4 *)g->slot, g->nhubs, g->max_degree, &ms))) return st;
     unsigned long long h[PGD_NSUMS];
     PGD_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_sums, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -1739,7 +1750,9 @@ pgd_status pgd_dev_decompose(pgd_graph *g, bool micro, pgd_counts *out) {
     for (int i = 0; i < PGD_NSUMS; i++) out->sums[i] = h[i];
     out->n = g->n;
     out->m = g->m;
-    out->kernel_ms = ms;
+    out->kernel_ms = ms.total;
+    out->hub_ms = ms.hub;
+    out->tri_ms = ms.tri;
     pgd_close_counts(out->sums, g->n, g->m, out->totals);
     g->has_micro = micro;
     return PGD_OK;
@@ -1981,7 +1994,7 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
     G.gnm = d_gnm;
     G.gdense = ndense_graphs ? d_gdense : nullptr;
     DenseView dv{(const uint64_t *)bits, d_wbase, d_bases, cn, d_cbase};
-    float ms = 0;
+    StageMs ms;
     BATCH_TRY(run_decompose(ctx, G, (int4 *)U.slot, U.nhubs, U.max_degree, &ms, ndense_graphs ? &dv : nullptr));
     std::vector<unsigned long long> h((size_t)k * PGD_NSUMS);
     if (cudaMemcpyAsync(h.data(), gsums, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s)) {
@@ -2003,7 +2016,9 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
         for (int j = 0; j < PGD_NSUMS; j++) o.sums[j] = h[(size_t)i * PGD_NSUMS + j];
         o.n = gnm[(size_t)2 * i];
         o.m = gnm[(size_t)2 * i + 1];
-        o.kernel_ms = ms;
+        o.kernel_ms = ms.total;
+        o.hub_ms = ms.hub;
+        o.tri_ms = ms.tri;
         pgd_close_counts(o.sums, o.n, o.m, o.totals);
         graphs[i]->has_micro = micro;
     }
@@ -2543,7 +2558,7 @@ pgd_status pgd_dev_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pai
     PB_CUDA(cudaMemcpyAsync(d_gdense, gdense.data(), (size_t)k, cudaMemcpyHostToDevice, s));
     PB_CUDA(cudaMemcpyAsync(d_wbase, wbase.data(), (size_t)k * sizeof(int64_t), cudaMemcpyHostToDevice, s));
     if (words > 0) PB_CUDA(cudaMemsetAsync(bits, 0, (size_t)words * sizeof(unsigned long long), s));
-    float ms = 0;
+    StageMs ms;
     if (M > 0) {
         PB_TRY(build_aux(U));
         if (words > 0)
@@ -2569,7 +2584,9 @@ pgd_status pgd_dev_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pai
         for (int j = 0; j < PGD_NSUMS; j++) o.sums[j] = h[(size_t)g * PGD_NSUMS + j];
         o.n = gnm[(size_t)2 * g];
         o.m = gnm[(size_t)2 * g + 1];
-        o.kernel_ms = ms;
+        o.kernel_ms = ms.total;
+        o.hub_ms = ms.hub;
+        o.tri_ms = ms.tri;
         pgd_close_counts(o.sums, o.n, o.m, o.totals);
     }
     cleanup();

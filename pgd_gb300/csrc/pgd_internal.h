@@ -20,6 +20,8 @@ struct pgd_ctx {
     unsigned long long *d_sums = nullptr;   // PGD_NSUMS
     unsigned long long *d_ctr = nullptr;    // work counters
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // stage events of a decomposition: triangle pass [evt0, evt1), k_hub [evh0, evh1)
+    cudaEvent_t evt0 = nullptr, evt1 = nullptr, evh0 = nullptr, evh1 = nullptr;
     unsigned long long launches = 0;        // kernels of this library launched
     // decomposition thresholds (results never depend on them; pgd_autotune sets them)
     int anchor_hub = 128;    // anchors of degree >= this take the bitmap (block) path

@@ -80,6 +80,12 @@ def lib():
         L.po_get_totals.argtypes = [_P, _U64P]
         L.po_get_micro.argtypes = [_P, _I64P, _I64P, _U64P]
         L.po_get_edge_tkc.argtypes = [_P, _U64P, _U64P, _U64P]
+        L.po_gen_rmat.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_uint64, _I32P, _I32P]
+        L.po_gen_rmat.restype = None
+        L.po_micro_row.argtypes = [ctypes.c_longlong, ctypes.c_longlong, ctypes.c_uint64, ctypes.c_uint64,
+                                   ctypes.c_uint64, _U64P]
+        L.po_micro_row.restype = None
         _lib = L
     return _lib
 
@@ -232,6 +238,27 @@ class OracleGraph:
         t, k, c = (np.zeros(m + 1, np.uint64) for _ in range(3))
         lib().po_get_edge_tkc(self.h, t, k, c)
         return t[:m], k[:m], c[:m]
+
+
+def rmat(scale, edge_factor=16, seed=1, a=0.57, b=0.19, c=0.19):
+    """Seeded RMAT pairs from the oracle's own generator (same draws as the
+    product's pgd_gen_rmat), for callers that must not load the product."""
+    k = edge_factor << scale
+    src = np.empty(k, np.int32)
+    dst = np.empty(k, np.int32)
+    lib().po_gen_rmat(scale, edge_factor, a, b, c, seed, src, dst)
+    return src, dst
+
+
+def micro_rows(dv, du, t, k4, c4):
+    """The 8 per-edge columns of each edge i from its endpoint degrees and
+    t, k4, c4 (the oracle's micro stores)."""
+    out = np.zeros((len(t), 8), np.uint64)
+    row = np.zeros(8, np.uint64)
+    for i in range(len(t)):
+        lib().po_micro_row(int(dv[i]), int(du[i]), int(t[i]), int(k4[i]), int(c4[i]), row)
+        out[i] = row
+    return out
 
 
 def close(sums, n, m):
