@@ -288,22 +288,26 @@ pgd_status pgd_autotune(pgd_ctx *ctx, pgd_graph *const *graphs, int k, int reps,
 
 /* ---- allocation-free decomposition --------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
- * memory when they need counts: code given a fixed workspace by a host
- * framework that forbids allocation, work recorded into a CUDA stream
- * capture (where cudaMalloc is not allowed), and latency-critical loops that
- * cannot afford cudaMalloc/cudaFree synchronising the device.
+ * memory when they need counts: a host framework that hands its plugins a
+ * fixed device workspace and forbids allocation (its memory manager owns the
+ * device), and latency-critical loops that cannot afford cudaMalloc/cudaFree,
+ * which can synchronise the whole device.
  *
  * Global counts of a graph already on the device as a CSR (d_off: n+1 int64,
- * d_adj: nnz int32; rows sorted, symmetric, no self loops or repeats), on
- * `stream` of `device`.  Every intermediate lives in one static device array
- * of pgd_noalloc_scratch_bytes() bytes (64 MiB) that the library reserves on
- * every GPU it is loaded on; the call never allocates.  Graphs that need
- * more scratch than that are refused with PGD_ENOMEM and a message in err.
- * The first call on a device looks up the array's address, so make it
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race and must be serialised by the caller.  Results (totals,
- * sums, n, m) go to the host struct *out; err (errlen bytes, may be NULL)
- * receives a message on failure. */
+ * d_adj: nnz int32; offsets from 0 to nnz, non-decreasing; rows sorted,
+ * symmetric, no self loops or repeats; anything else is refused with
+ * PGD_EINVAL), on `stream` of `device`.  Every intermediate lives in one
+ * static device array of pgd_noalloc_scratch_bytes() bytes (64 MiB) that the
+ * library reserves on every GPU it is loaded on; the call never allocates.
+ * Graphs that need more scratch than that are refused with PGD_ENOMEM and a
+ * message in err.  The first call on a device looks up the array's address,
+ * so make it before any stream capture.  All calls share the array and each
+ * clears what must start at zero: calls that overlap on the GPU race and must
+ * be serialised by the caller.  The call synchronises `stream` up to four
+ * times, because later launch sizes (hub-anchored edges, work items) are read
+ * back to the host, and it leaves the calling thread's current device as it
+ * found it.  Results (totals, sums, n, m) go to the host struct *out; err
+ * (errlen bytes, may be NULL) receives a message on failure. */
 pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int32_t *d_adj, int64_t n, int64_t nnz,
                                      int device, void *stream, pgd_counts *out, char *err, size_t errlen);
 uint64_t pgd_noalloc_scratch_bytes(void);

@@ -2058,6 +2058,18 @@ constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
 unsigned char *g_noalloc_addr[kNoAllocMaxDevices] = {};
 
+// Offsets must start at 0, end at nnz and never decrease; checked before
+// anything indexes the adjacency through them.
+__global__ void k_na_offsets(const int64_t *off, int64_t n, int64_t nnz, unsigned long long *bad) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t a = off[v], b = off[v + 1];
+        bool ok = a <= b && a >= 0 && b <= nnz;
+        if (v == 0) ok = ok && a == 0;
+        if (v == n - 1) ok = ok && b == nnz;
+        if (!ok) atomicAdd(bad, 1ull);
+    }
+}
+
 // Rows must be sorted, in range, free of self loops, and symmetric.
 __global__ void k_na_check(const int64_t *off, const int32_t *adj, const int32_t *row, int64_t n, int64_t nnz,
                            unsigned long long *bad) {
@@ -2105,6 +2117,20 @@ struct Carve {
     }
 };
 
+// Restores the calling thread's current device on every return path.
+struct DeviceRestore {
+    int prev = -1;
+    DeviceRestore() {
+        if (cudaGetDevice(&prev) != cudaSuccess) {
+            prev = -1;
+            cudaGetLastError();
+        }
+    }
+    ~DeviceRestore() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
 void na_msg(char *err, size_t errlen, const std::string &m) {
     if (err && errlen) {
         size_t k = std::min(errlen - 1, m.size());
@@ -2138,6 +2164,7 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
         return PGD_EINVAL;
     }
     cudaStream_t s = (cudaStream_t)stream_;
+    DeviceRestore restore_device;
     NA_CUDA(cudaSetDevice(device));
     unsigned char *base = nullptr;
     {
@@ -2224,11 +2251,18 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
         pgd_close_counts(out->sums, n, m, out->totals);
         return PGD_OK;
     }
-    // validate and derive the per-graph structures
+    // validate the offsets, then the rows, then derive the per-graph structures
+    unsigned long long bad = 0;
+    k_na_offsets<<<grid_for(n), kThreads, 0, s>>>(d_off, n, nnz, ctr + 4);
+    NA_CUDA(cudaMemcpyAsync(&bad, ctr + 4, sizeof(bad), cudaMemcpyDeviceToHost, s));
+    NA_CUDA(cudaStreamSynchronize(s));
+    if (bad) {
+        na_msg(err, errlen, "device CSR rejected: offsets must start at 0, end at nnz and never decrease");
+        return PGD_EINVAL;
+    }
     k_rows<<<grid_for(nnz), kThreads, 0, s>>>(d_off, n, nnz, row);
     k_na_check<<<grid_for(nnz), kThreads, 0, s>>>(d_off, d_adj, row, n, nnz, ctr + 3);
     k_na_degrees<<<grid_for(n), kThreads, 0, s>>>(d_off, n, deg);
-    unsigned long long bad = 0;
     NA_CUDA(cudaMemcpyAsync(&bad, ctr + 3, sizeof(bad), cudaMemcpyDeviceToHost, s));
     NA_CUDA(cudaStreamSynchronize(s));
     if (bad) {
