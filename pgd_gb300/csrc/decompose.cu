@@ -513,42 +513,6 @@ __device__ __forceinline__ bool in_t(const uint32_t *Rw, const RankBits &bm, con
     return th.count >= 0 ? pgd_contains(th.ids, th.count, y) : pgd_contains(Nq, dq, y);
 }
 
-// Histogram of the hub ids in the lists of the 32 vertices the warp holds
-// (one per lane, len entries at list): long lists warp-cooperatively, the
-// rest flattened.  H is a shared or a global pointer (distinct code paths so
-// that shared-memory atomics stay shared).
-// Returns the number of entries visited (the same in every lane).
-template <typename AddFn>
-__device__ __forceinline__ int hist_lists(const int32_t *list, int len, int lane, AddFn add) {
-    int visited = __reduce_add_sync(0xffffffffu, (unsigned)len);
-    unsigned longm = __ballot_sync(0xffffffffu, len >= 64);
-    while (longm) {
-        const int src = __ffs(longm) - 1;
-        longm &= longm - 1;
-        const int32_t *L = (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)list, src);
-        const int ln = __shfl_sync(0xffffffffu, len, src);
-        int i = lane;
-        for (; i + 32 < ln; i += 64) {
-            const int32_t h0 = __ldg(L + i), h1 = __ldg(L + i + 32);
-            add(h0);
-            add(h1);
-        }
-        if (i < ln) add(__ldg(L + i));
-    }
-    if (len >= 64) len = 0;
-    const int incl = pgd_warp_incl_scan(len);
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    const int excl = incl - len;
-    for (int b2 = 0; b2 < total; b2 += 32) {
-        const int it = b2 + lane;
-        const int own = owner_of(incl, it);
-        const int32_t *olist = (const int32_t *)__shfl_sync(0xffffffffu, (unsigned long long)list, own);
-        const int oexcl = __shfl_sync(0xffffffffu, excl, own);
-        if (it < total) add(__ldg(olist + (it - oexcl)));
-    }
-    return visited;
-}
-
 __device__ __forceinline__ int64_t rec_off(const int4 &ra) { return (int64_t)(((uint64_t)(uint32_t)ra.y << 32) | (uint32_t)ra.x); }
 __device__ __forceinline__ int64_t rec_offp(const int4 &ra) { return (int64_t)(((uint64_t)(uint32_t)ra.w << 32) | (uint32_t)ra.z); }
 
@@ -581,10 +545,89 @@ __device__ __forceinline__ void plan_entry(const DevGraph &G, bool inT, const in
     }
 }
 
+// Shared-memory scratch of walk_lists: 1024 inclusive prefix sums, 1024
+// list starts and 32 warp totals (k_hub lends its per-warp T bitmaps, which
+// are idle while an item's histogram is built; 3,104 words in all).
+struct WalkScratch {
+    int *pre;               // [1024]
+    const int32_t **ptr;    // [1024]
+    int *wtot;              // [32]
+};
+constexpr int kWalkScratchWords = 1024 + 2 * 1024 + 32;
+
+// First t in [0, 1024) with pre[t] > i (pre non-decreasing; pre[1023] > i).
+__device__ __forceinline__ int walk_owner_search(const int *pre, int i) {
+    int lo = 0;
+#pragma unroll
+    for (int step = 512; step > 0; step >>= 1)
+        if (pre[lo + step - 1] <= i) lo += step;
+    return lo;
+}
+
+// Applies fn(h) to every entry h of the hub-neighbour lists of N(p) (and, when
+// bm is given, marks N(p) in the rank bitmap), balanced over the whole CTA:
+// the lists of 1024 entries of N(p) at a time are concatenated, and each warp
+// takes an equal contiguous share of their entries, so that a few long lists
+// no longer keep the other warps waiting at the item's barrier.  Inside a
+// share, the owner list of each entry is found from 32 prefix sums held one
+// per lane (a 5-step search), two entries per lane in flight.  All threads of
+// the CTA must call; returns the number of entries visited.
+template <typename Fn>
+__device__ __forceinline__ long long walk_lists(const DevGraph &G, const int32_t *Np, const int32_t *Rp, int dp,
+                                                const RankBits *bm, const WalkScratch &W, Fn fn) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    long long visited = 0;
+    for (int c0 = 0; c0 < dp; c0 += kHubWarps * 32) {
+        const int j = c0 + (int)threadIdx.x;
+        int len = 0;
+        const int32_t *list = nullptr;
+        if (j < dp) {
+            const int32_t x = __ldg(Np + j);
+            if (bm) bm->set(__ldg(Rp + j));
+            const int64_t o = G.offh[x];
+            len = (int)(G.offh[x + 1] - o);
+            list = G.adjh + o;
+        }
+        const int incl = pgd_warp_incl_scan(len);
+        if (lane == 31) W.wtot[wid] = incl;
+        __syncthreads();
+        const int wt = W.wtot[lane];
+        const int wincl = pgd_warp_incl_scan(wt);
+        const int total = __shfl_sync(0xffffffffu, wincl, 31);
+        W.pre[threadIdx.x] = __shfl_sync(0xffffffffu, wincl - wt, wid) + incl;
+        W.ptr[threadIdx.x] = list;
+        __syncthreads();
+        visited += total;
+        const int share = (total + kHubWarps - 1) / kHubWarps;
+        const int lo = min(total, wid * share), hi = min(total, lo + share);
+        int base = lo < hi ? walk_owner_search(W.pre, lo) : 0;
+        for (int s = lo; s < hi; s += 64) {
+            const int cand = base + lane < 1024 ? W.pre[base + lane] : 0x7fffffff;
+            const int last = __shfl_sync(0xffffffffu, cand, 31);
+            const int iA = s + lane, iB = s + 32 + lane;
+            const bool vA = iA < hi, vB = iB < hi;
+            // owners beyond base + 31 (a run of empty lists): full search
+            int ownA = base + owner_of(cand, iA), ownB = base + owner_of(cand, iB);
+            if (vA && iA >= last) ownA = walk_owner_search(W.pre, iA);
+            if (vB && iB >= last) ownB = walk_owner_search(W.pre, iB);
+            int32_t hA = 0, hB = 0;
+            if (vA) hA = __ldg(W.ptr[ownA] + (iA - (ownA ? W.pre[ownA - 1] : 0)));
+            if (vB) hB = __ldg(W.ptr[ownB] + (iB - (ownB ? W.pre[ownB - 1] : 0)));
+            if (vA) fn(hA);
+            if (vB) fn(hB);
+            // the next step's first entry (s + 64) belongs to lane 31's second
+            // owner or a later list; the loop ends when that entry is invalid
+            base = __shfl_sync(0xffffffffu, ownB, 31);
+        }
+        __syncthreads();
+    }
+    return visited;
+}
+
 __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
     extern __shared__ __align__(16) uint32_t s_dyn[];
     __shared__ unsigned long long s_red[kHubWarps][PGD_NSUMS];
-    __shared__ uint32_t s_R[kHubWarps][kRankBits / 32];
+    __shared__ __align__(16) uint32_t s_R[kHubWarps][kRankBits / 32];
     __shared__ long long s_item;
     __shared__ int s_enext;
     __shared__ unsigned long long s_hcount;
@@ -592,6 +635,12 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     uint32_t *Rw = s_R[wid];
     for (int i = lane; i < kRankBits / 32; i += 32) Rw[i] = 0;
+    static_assert(kWalkScratchWords <= kHubWarps * (kRankBits / 32), "walk scratch exceeds the T bitmaps");
+    WalkScratch walk;
+    uint32_t *const s_flat = &s_R[0][0];
+    walk.pre = (int *)s_flat;
+    walk.ptr = (const int32_t **)(s_flat + 1024);
+    walk.wtot = (int *)(s_flat + 3072);
     const bool smem_hist = A.smem_hist != 0;
     // dynamic shared memory: [histogram (when shared)][rank bitmap, ranks < split]
     uint32_t *sh_hist = s_dyn;
@@ -640,25 +689,16 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
         const int32_t *Rp = G.adj_rank + G.off[p];
 
         // ---- (1) N(p) bitmap and the W histogram --------------------------
+        // (the walk borrows the T bitmaps as scratch and they are zeroed again
+        // before the edges, which need them clear)
         {
-            unsigned long long visited = 0;
-            for (int base = wid * 32; base < dp; base += kHubWarps * 32) {
-                const int j = base + lane;
-                int len = 0;
-                const int32_t *list = nullptr;
-                if (j < dp) {
-                    const int32_t x = __ldg(Np + j);
-                    bm.set(__ldg(Rp + j));
-                    const int64_t o = G.offh[x];
-                    len = (int)(G.offh[x + 1] - o);
-                    list = G.adjh + o;
-                }
-                if (smem_hist)
-                    visited += hist_lists(list, len, lane, [&](int32_t h) { atomicAdd(sh_hist + hw(h), hinc(h)); });
-                else
-                    visited += hist_lists(list, len, lane, [&](int32_t h) { atomicAdd(gl_hist + hw(h), hinc(h)); });
-            }
-            if (lane == 0 && visited) atomicAdd(&s_hcount, visited);
+            long long visited;
+            if (smem_hist)
+                visited = walk_lists(G, Np, Rp, dp, &bm, walk, [&](int32_t h) { atomicAdd(sh_hist + hw(h), hinc(h)); });
+            else
+                visited = walk_lists(G, Np, Rp, dp, &bm, walk, [&](int32_t h) { atomicAdd(gl_hist + hw(h), hinc(h)); });
+            if (threadIdx.x == 0) s_hcount = (unsigned long long)visited;
+            for (int i = threadIdx.x; i < kWalkScratchWords; i += blockDim.x) s_flat[i] = 0;
         }
         __syncthreads();
 
@@ -811,25 +851,17 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
         }
         __syncthreads();
         for (int i = threadIdx.x; i < dp; i += blockDim.x) bm.clear_word(__ldg(Rp + i));
-        if (s_hcount * 4 >= (unsigned long long)A.nhubs) {
+        if (smem_hist || s_hcount * 4 >= (unsigned long long)A.nhubs) {
+            // a shared histogram is cleared whole: a few 16-byte stores per thread
             uint4 *h4 = (uint4 *)(smem_hist ? sh_hist : gl_hist);
             for (int i = threadIdx.x; i < nh4; i += blockDim.x) h4[i] = make_uint4(0, 0, 0, 0);
         } else {
-            // few entries touched (large graphs, small anchors): clear just those
-            for (int base = wid * 32; base < dp; base += kHubWarps * 32) {
-                const int j = base + lane;
-                int len = 0;
-                const int32_t *list = nullptr;
-                if (j < dp) {
-                    const int32_t x = __ldg(Np + j);
-                    const int64_t o = G.offh[x];
-                    len = (int)(G.offh[x + 1] - o);
-                    list = G.adjh + o;
-                }
-                // (a shared 16-bit word's other counter is zero or cleared too)
-                if (smem_hist) hist_lists(list, len, lane, [&](int32_t h) { sh_hist[hw(h)] = 0; });
-                else hist_lists(list, len, lane, [&](int32_t h) { gl_hist[hw(h)] = 0; });
-            }
+            // few entries of a global histogram touched (large graphs, small
+            // anchors): clear just those (a 16-bit word's other counter is zero
+            // or cleared too); the walk's scratch is zeroed by the next item's
+            // phase 1 before any edge reads the T bitmaps
+            __syncthreads();
+            walk_lists(G, Np, Rp, dp, nullptr, walk, [&](int32_t h) { gl_hist[hw(h)] = 0; });
         }
         __syncthreads();
     }
