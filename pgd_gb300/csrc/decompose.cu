@@ -56,7 +56,8 @@ constexpr int kThreads = 256;
 constexpr int kHubWarps = 32;            // hub-anchor CTA: 1024 threads (latency-bound gathers want warps)
 constexpr int kLightWarps = 8;           // light path: 256 threads, one edge per warp
 constexpr int kAnchorHub = 128;          // default: anchors of degree >= this take the bitmap path
-constexpr int kCacheHub = 64;            // default: W(w,p) from the histogram for neighbours of degree >= this
+constexpr int kCacheHub = 64;            // allocation-free path: W(w,p) from the histogram for degree >= this
+constexpr int kWideHub = 256;            // hubs of lower degree get 8-bit histogram counters (W(w,p) <= degree)
 constexpr int kLightStageMax = 256;      // largest warp/block threshold the light path can stage
 constexpr int kChunk = 8192;             // edges of one anchor per CTA work item (target; measured
                                          // 2048: +9 %, 6144-12288: flat)
@@ -239,6 +240,25 @@ __global__ void k_hub_flags(const int32_t *deg, int64_t n, int cache_hub, uint32
 __global__ void k_hub_ids(const uint32_t *flag, const uint32_t *pos, int64_t n, int32_t *hubid) {
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
         hubid[v] = flag[v] ? (int32_t)pos[v] : -1;
+}
+
+// Hub ids in two tiers of the W histogram: vertices of degree >= wide (16- or
+// 32-bit counters) get ids 0..nA-1, those of degree in [cache_hub, wide)
+// (8-bit counters: W(w,p) <= deg(w) < 256) get nA.. in id order.
+__global__ void k_hub_tier_flags(const int32_t *deg, int64_t n, int cache_hub, int wide, uint32_t *flag_a,
+                                 uint32_t *flag_b) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int d = deg[v];
+        flag_a[v] = d >= cache_hub && d >= wide ? 1u : 0u;
+        flag_b[v] = d >= cache_hub && d < wide ? 1u : 0u;
+    }
+}
+
+__global__ void k_hub_tier_ids(const uint32_t *flag_a, const uint32_t *pos_a, const uint32_t *flag_b,
+                               const uint32_t *pos_b, int64_t n, int32_t *hubid) {
+    const uint32_t na = pos_a[n];
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        hubid[v] = flag_a[v] ? (int32_t)pos_a[v] : (flag_b[v] ? (int32_t)(na + pos_b[v]) : -1);
 }
 
 // t of every edge (or of the edges at the E_ordered positions listed in pos),
@@ -462,9 +482,11 @@ struct HubArgs {
     int64_t nitems;
     uint32_t *ghist;          // per CTA histogram slices (hstride words each) when not in shared memory
     int32_t nhubs;
+    int32_t nwide;            // hub ids below this: wide counters; the rest 8-bit, four per word
+    int64_t wide_words;       // words of the wide tier (the 8-bit tier follows)
     int64_t hstride;
     int smem_hist;
-    int hist16;               // two 16-bit counters per word (every W < 65536: max degree below that)
+    int hist16;               // wide counters of 16 bits, two per word (every W < 65536: max degree below that)
     uint32_t *gbitmap;        // per CTA rank-bitmap slices (nwords each) when split < n
     int64_t nwords;
     int32_t split;            // ranks below this are kept in shared memory
@@ -655,10 +677,18 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
     unsigned long long *acc = s_red[wid];
     if (lane < PGD_NSUMS) acc[lane] = 0;
     const int nh4 = (int)(A.hstride >> 2);
-    // counter h: word and increment (16-bit halves never carry: W < 65536)
-    auto hw = [h16](int32_t h) { return h16 ? (h >> 1) : h; };
-    auto hinc = [h16](int32_t h) { return h16 ? (1u << ((h & 1) << 4)) : 1u; };
-    auto hval = [h16](uint32_t word, int32_t h) { return h16 ? ((word >> ((h & 1) << 4)) & 0xffffu) : word; };
+    // counter h: word and increment.  Wide tier (h < nwide): 16-bit halves
+    // (never carry: W < 65536) or whole words; 8-bit tier: bytes (never carry:
+    // W(w,p) <= deg(w) < 256)
+    const int32_t nwide = A.nwide;
+    const int32_t wwords = (int32_t)A.wide_words;
+    auto hw = [=](int32_t h) { return h < nwide ? (h16 ? (h >> 1) : h) : wwords + ((h - nwide) >> 2); };
+    auto hinc = [=](int32_t h) {
+        return h < nwide ? (h16 ? (1u << ((h & 1) << 4)) : 1u) : (1u << (((h - nwide) & 3) << 3));
+    };
+    auto hval = [=](uint32_t word, int32_t h) {
+        return h < nwide ? (h16 ? ((word >> ((h & 1) << 4)) & 0xffffu) : word) : ((word >> (((h - nwide) & 3) << 3)) & 0xffu);
+    };
     int cur_g = -1;
     for (int i = threadIdx.x; i < (A.split >> 5); i += blockDim.x) bm.s[i] = 0;
     {
@@ -1463,17 +1493,23 @@ static pgd_status build_aux(pgd_graph *g) {
     pgd_tmp_free(ctx, tmp);
     PGD_LAUNCH(ctx, k_oriented_fill, grid_for(std::max(nnz, n + 1)), kThreads, 0, g->off, g->adj, flag, pos, n, nnz,
                g->offp, g->adjp);
-    // hub ids
-    PGD_LAUNCH(ctx, k_hub_flags, grid_for(n), kThreads, 0, g->deg, n, ctx->cache_hub, flag);
+    // hub ids, wide tier first
+    uint32_t *flag_b = nullptr, *pos_b = nullptr;
+    if ((st = tg.alloc(&flag_b, (n + 1) * sizeof(uint32_t)))) return st;
+    if ((st = tg.alloc(&pos_b, (n + 1) * sizeof(uint32_t)))) return st;
+    PGD_LAUNCH(ctx, k_hub_tier_flags, grid_for(n), kThreads, 0, g->deg, n, ctx->cache_hub, kWideHub, flag, flag_b);
     PGD_CUDA(ctx, cudaMemsetAsync(flag + n, 0, sizeof(uint32_t), s));
+    PGD_CUDA(ctx, cudaMemsetAsync(flag_b + n, 0, sizeof(uint32_t), s));
     tb = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, tb, flag, pos, n + 1, s);
     if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
     cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, n + 1, s);
+    cub::DeviceScan::ExclusiveSum(tmp, tb, flag_b, pos_b, n + 1, s);
     pgd_tmp_free(ctx, tmp);
-    PGD_LAUNCH(ctx, k_hub_ids, grid_for(n), kThreads, 0, flag, pos, n, g->hubid);
-    uint32_t nh = 0;
-    PGD_CUDA(ctx, cudaMemcpyAsync(&nh, pos + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    PGD_LAUNCH(ctx, k_hub_tier_ids, grid_for(n), kThreads, 0, flag, pos, flag_b, pos_b, n, g->hubid);
+    uint32_t nh_a = 0, nh_b = 0;
+    PGD_CUDA(ctx, cudaMemcpyAsync(&nh_a, pos + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    PGD_CUDA(ctx, cudaMemcpyAsync(&nh_b, pos_b + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     // hub-neighbour lists (their length depends on the hub threshold)
     PGD_LAUNCH(ctx, k_hubnb_flags, grid_for(nnz), kThreads, 0, g->adj, g->hubid, nnz, flag);
     PGD_CUDA(ctx, cudaMemsetAsync(flag + nnz, 0, sizeof(uint32_t), s));
@@ -1525,7 +1561,8 @@ static pgd_status build_aux(pgd_graph *g) {
         PGD_LAUNCH(ctx, k_top_rows, grid_for(32 * n), kThreads, 0, g->offp, g->adjp_rank, g->vrank, n, g->top_r,
                    g->toprows);
     PGD_CUDA(ctx, cudaStreamSynchronize(s));
-    g->nhubs = (int32_t)nh;
+    g->nhubs = (int32_t)(nh_a + nh_b);
+    g->nhubs_wide = (int32_t)nh_a;
     PGD_CUDA(ctx, cudaGetLastError());
     g->aux_cache_hub = ctx->cache_hub;
     g->has_aux = true;
@@ -1578,11 +1615,13 @@ struct DenseView {
 // (atomics) in shared memory when it fits, then as many bitmap ranks as the
 // remaining shared memory holds; per-CTA global slices for the rest.  Fills
 // the layout fields of H and returns the dynamic shared memory size.
-static size_t hub_layout(int64_t n, int32_t nhubs, int32_t max_degree, HubArgs *H) {
+static size_t hub_layout(int64_t n, int32_t nhubs, int32_t nwide, int32_t max_degree, HubArgs *H) {
     H->nwords = (n + 31) / 32;
     H->nhubs = nhubs;
+    H->nwide = nwide;
     H->hist16 = max_degree < 65536 ? 1 : 0;
-    const int64_t hwords = H->hist16 ? ((int64_t)nhubs + 1) / 2 : (int64_t)nhubs;
+    H->wide_words = H->hist16 ? ((int64_t)nwide + 1) / 2 : (int64_t)nwide;
+    const int64_t hwords = H->wide_words + ((int64_t)(nhubs - nwide) + 3) / 4;
     H->hstride = std::max<int64_t>(4, (hwords + 3) & ~(int64_t)3);
     H->smem_hist = H->hstride * 4 <= kMaxDynSmem ? 1 : 0;
     const int64_t rem_words = kMaxDynSmem / 4 - (H->smem_hist ? H->hstride : 0);
@@ -1596,7 +1635,8 @@ struct StageMs {
     float total = 0, tri = 0, hub = 0;
 };
 
-static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int32_t nhubs, int32_t max_degree,
+static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int32_t nhubs, int32_t nwide,
+                                int32_t max_degree,
                                 StageMs *ms, const DenseView *dense = nullptr) {
     cudaStream_t s = ctx->stream;
     pgd_status st;
@@ -1659,7 +1699,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     // other edges.  Hub-anchored edges grouped by anchor, the rest one warp each
     // (dense-graph edges need none).
     HubArgs H;
-    const size_t smem = hub_layout(G.n, nhubs, max_degree, &H);
+    const size_t smem = hub_layout(G.n, nhubs, nwide, max_degree, &H);
     PGD_CUDA(ctx, cudaEventRecord(ctx->evt0, s));
     if (sampled) PGD_LAUNCH(ctx, k_tslot, grid_for(32 * G.m), kThreads, 0, G, slot, nullptr, 0);
     if (nitems > 0) {
@@ -1775,7 +1815,7 @@ pgd_status pgd_dev_decompose(pgd_graph *g, bool micro, pgd_counts *out) {
     if ((!g->has_aux || g->aux_cache_hub != ctx->cache_hub) && (st = build_aux(g))) return st;
     PGD_CUDA(ctx, cudaMemsetAsync(ctx->d_sums, 0, PGD_NSUMS * sizeof(unsigned long long), s));
     StageMs ms;
-    if ((st = run_decompose(ctx, dev_view(g, micro), (int4 *)g->slot, g->nhubs, g->max_degree, &ms))) return st;
+    if ((st = run_decompose(ctx, dev_view(g, micro), (int4 *)g->slot, g->nhubs, g->nhubs_wide, g->max_degree, &ms))) return st;
     unsigned long long h[PGD_NSUMS];
     PGD_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_sums, sizeof(h), cudaMemcpyDeviceToHost, s));
     PGD_CUDA(ctx, cudaStreamSynchronize(s));
@@ -2027,7 +2067,7 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
     G.gdense = ndense_graphs ? d_gdense : nullptr;
     DenseView dv{(const uint64_t *)bits, d_wbase, d_bases, cn, d_cbase};
     StageMs ms;
-    BATCH_TRY(run_decompose(ctx, G, (int4 *)U.slot, U.nhubs, U.max_degree, &ms, ndense_graphs ? &dv : nullptr));
+    BATCH_TRY(run_decompose(ctx, G, (int4 *)U.slot, U.nhubs, U.nhubs_wide, U.max_degree, &ms, ndense_graphs ? &dv : nullptr));
     std::vector<unsigned long long> h((size_t)k * PGD_NSUMS);
     if (cudaMemcpyAsync(h.data(), gsums, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s)) {
         cleanup();
@@ -2258,7 +2298,7 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     // the largest possible count (the maximum degree is not known here
     // either: 32-bit counters)
     HubArgs H;
-    hub_layout(n, (int32_t)hub_bound, 1 << 30, &H);
+    hub_layout(n, (int32_t)hub_bound, (int32_t)hub_bound, 1 << 30, &H);
     // fewer hubs never need more global memory: a histogram that fits in
     // shared memory for hub_bound hubs fits for fewer, and the bitmap's
     // shared part only grows
@@ -2376,7 +2416,7 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     }
     if (nitems > 0) {
         // the layout for the actual hub count (the carve above covers it)
-        const size_t smem = hub_layout(n, (int32_t)nhubs, 1 << 30, &H);
+        const size_t smem = hub_layout(n, (int32_t)nhubs, (int32_t)nhubs, 1 << 30, &H);
         if ((!H.smem_hist && !ghist) || ((int64_t)H.split < n && !gbm)) {
             na_msg(err, errlen, "internal: k_hub layout needs a global slice that was not carved");
             return PGD_ECUDA;
@@ -2639,7 +2679,7 @@ pgd_status pgd_dev_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pai
         G.gnm = d_gnm;
         G.gdense = ndense_graphs ? d_gdense : nullptr;
         DenseView dv{(const uint64_t *)bits, d_wbase, d_vbase, cn, d_cbase};
-        PB_TRY(run_decompose(ctx, G, (int4 *)U->slot, U->nhubs, U->max_degree, &ms, ndense_graphs ? &dv : nullptr));
+        PB_TRY(run_decompose(ctx, G, (int4 *)U->slot, U->nhubs, U->nhubs_wide, U->max_degree, &ms, ndense_graphs ? &dv : nullptr));
     }
     std::vector<unsigned long long> h((size_t)k * PGD_NSUMS);
     PB_CUDA(cudaMemcpyAsync(h.data(), gsums, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));

@@ -25,7 +25,7 @@ struct pgd_ctx {
     unsigned long long launches = 0;        // kernels of this library launched
     // decomposition thresholds (results never depend on them; pgd_autotune sets them)
     int anchor_hub = 128;    // anchors of degree >= this take the bitmap (block) path
-    int cache_hub = 64;      // W(w,p) taken from the per-anchor histogram for neighbours of degree >= this
+    int cache_hub = 40;      // W(w,p) taken from the per-anchor histogram for neighbours of degree >= this
     int dense_max = 2048;    // batched graphs with at most this many vertices use row bitsets
 };
 
@@ -67,6 +67,7 @@ struct pgd_graph {
     int32_t *adjp = nullptr;          // m: neighbours of higher (degree, id)
     int32_t *hubid = nullptr;         // n: slot in the W histogram, -1 if none
     int32_t nhubs = 0;
+    int32_t nhubs_wide = 0;           // hub ids below this have wide (16/32-bit) counters, the rest 8-bit
     int32_t aux_cache_hub = 0;        // threshold the hub ids were built with
     int64_t *offh = nullptr;          // n+1: hub-neighbour lists
     int32_t *adjh = nullptr;          // nadjh: hub ids of each vertex's hub neighbours
