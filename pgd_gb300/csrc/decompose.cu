@@ -623,7 +623,29 @@ __device__ __forceinline__ long long walk_lists(const DevGraph &G, const int32_t
         const int share = (total + kHubWarps - 1) / kHubWarps;
         const int lo = min(total, wid * share), hi = min(total, lo + share);
         int base = lo < hi ? walk_owner_search(W.pre, lo) : 0;
-        for (int s = lo; s < hi; s += 64) {
+        for (int s = lo; s < hi;) {
+            // most entries sit in long lists: while one list covers the next
+            // 128 (or 64) entries, take them straight, coalesced, 4 (2) per lane
+            const int own_end = W.pre[base];
+            if (own_end - s >= 64 && hi - s >= 64) {
+                const int32_t *L = W.ptr[base] + (s - (base ? W.pre[base - 1] : 0));
+                if (own_end - s >= 128 && hi - s >= 128) {
+                    const int32_t h0 = __ldg(L + lane), h1 = __ldg(L + 32 + lane), h2 = __ldg(L + 64 + lane),
+                                  h3 = __ldg(L + 96 + lane);
+                    fn(h0);
+                    fn(h1);
+                    fn(h2);
+                    fn(h3);
+                    s += 128;
+                } else {
+                    const int32_t h0 = __ldg(L + lane), h1 = __ldg(L + 32 + lane);
+                    fn(h0);
+                    fn(h1);
+                    s += 64;
+                }
+                if (s >= own_end) base = s < hi ? walk_owner_search(W.pre, s) : base;
+                continue;
+            }
             const int cand = base + lane < 1024 ? W.pre[base + lane] : 0x7fffffff;
             const int last = __shfl_sync(0xffffffffu, cand, 31);
             const int iA = s + lane, iB = s + 32 + lane;
@@ -640,6 +662,7 @@ __device__ __forceinline__ long long walk_lists(const DevGraph &G, const int32_t
             // the next step's first entry (s + 64) belongs to lane 31's second
             // owner or a later list; the loop ends when that entry is invalid
             base = __shfl_sync(0xffffffffu, ownB, 31);
+            s += 64;
         }
         __syncthreads();
     }
