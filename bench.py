@@ -248,6 +248,11 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--batched-graphs", type=int, default=4096)
+    ap.add_argument("--served-requests", type=int, default=2000)
+    ap.add_argument("--served-rates", default="4000,1000000")
     args = ap.parse_args()
 
     if args.impl == "reference":
@@ -423,6 +428,38 @@ def main():
                          (stride, args.order, k, m, sec)}
         log("cpu baseline (%s, %d threads): %.3g edges/s" % (kind, threads, k / sec))
 
+    # ---- the second half of the metric: batched and served graphs/s -------
+    # (rank 0 at N = 1; wall-clock throughput through the public API, each
+    # result checked against the plain one-graph-per-call path and a
+    # stratified sample against the oracle, outside the timed regions)
+    batched = served = None
+    if rank == 0 and world == 1:
+        from benchmarks import suite
+
+        if not args.no_batched:
+            b = suite.run_batch(argparse.Namespace(graphs=args.batched_graphs, seed=1, reps=2, plain_sample=256),
+                                emit=False)
+            batched = {k_: b[k_] for k_ in (
+                "graphs", "pairs", "seconds", "graphs_per_s", "plain_graphs", "plain_graphs_per_s",
+                "speedup_vs_single_graph_api", "speedup_vs_batch_of_one", "mismatches_vs_plain", "oracle_checked",
+                "oracle_mismatches", "thresholds", "workload")}
+            batched["unit"] = "graphs/s"
+            log("batched: %.0f graphs/s, %.1fx the single-graph API, %.1fx the batch kernels one graph per call"
+                % (b["graphs_per_s"], b["speedup_vs_single_graph_api"], b["speedup_vs_batch_of_one"]))
+        if not args.no_served:
+            lines = suite.run_serve(argparse.Namespace(requests=args.served_requests, seed=1, rates=args.served_rates,
+                                                       rate=4000.0, workers=2), emit=False)
+            served = {"unit": "graphs/s", "workload": lines[0]["workload"], "requests": lines[0]["requests"],
+                      "plain_graphs_per_s": lines[0]["plain_graphs_per_s"],
+                      "oracle_checked": lines[0]["oracle_checked"], "oracle_mismatches": lines[0]["oracle_mismatches"],
+                      "rates": [{k_: ln[k_] for k_ in (
+                          "offered_rate", "graphs_per_s", "p50_ms", "p99_ms", "queue_p50_ms", "queue_p99_ms",
+                          "service_p50_ms", "service_p99_ms", "speedup_vs_best_plain", "mismatches_vs_plain",
+                          "batches", "skipped_ahead")} for ln in lines]}
+            for ln in lines:
+                log("served at %.0f/s offered: %.0f graphs/s, p50 %.2f ms, p99 %.2f ms, %.1fx the plain loop"
+                    % (ln["offered_rate"], ln["graphs_per_s"], ln["p50_ms"], ln["p99_ms"], ln["speedup_vs_best_plain"]))
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -431,6 +468,7 @@ def main():
             "config": workload_config(args.scale, args.order, n, m), "roofline": roofline,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
             "totals": {k_: int(v) for k_, v in zip(pgd.TOTAL_NAMES, ref_totals)},
+            "batched": batched, "served": served,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -1,11 +1,11 @@
-"""Benchmarks of the batched and served decomposition paths.
+"""Benchmarks of the batched, served, large and small configurations.
 
-    python -m pgd_gb300.benchmarks batch [--graphs 4096] [--seed 1]
-    python -m pgd_gb300.benchmarks serve [--requests 2000] [--rate 4000 | --rates 1000,4000,...] [--seed 1]
-    python -m pgd_gb300.benchmarks large [--workloads rmat24,rgg24] [--samples 1000]
-    python -m pgd_gb300.benchmarks profile [--scale 18] [--order kcore] [--reps 1]
-    python -m pgd_gb300.benchmarks small [--reps 50]
-    python -m pgd_gb300.benchmarks profile_batch [--graphs 256]
+    python -m benchmarks.suite batch [--graphs 4096] [--seed 1]
+    python -m benchmarks.suite serve [--requests 2000] [--rate 4000 | --rates 1000,4000,...] [--seed 1]
+    python -m benchmarks.suite large [--workloads rmat24,rgg24] [--samples 1000]
+    python -m benchmarks.suite profile [--scale 18] [--order kcore] [--reps 1]
+    python -m benchmarks.suite small [--reps 50]
+    python -m benchmarks.suite profile_batch [--graphs 256]
 
 batch: 4096 independent graphs, n uniform in [16, 2048]; half G(n, p) with p
 uniform in [0.01, 0.5], half Barabasi-Albert with m uniform in {2..8}; all
@@ -41,8 +41,10 @@ profile: one RMAT graph of the given scale, k-core order, decomposed `reps`
 times with per-edge counts; prints the kernel time of each run.  This is the
 command the ncu captures of the decomposition kernels are taken on.
 
-Every batch/serve result is checked against the plain path's counts.  Prints
-one JSON line per mode (per workload for `large`).
+Every batch/serve result is checked against the plain path's counts, and a
+stratified sample of the graphs (spread over sizes, up to 20,000 edges each)
+against the oracle (tests/oracle_lib.py, outside every timed region).
+Prints one JSON line per mode (per workload for `large`).
 """
 import argparse
 import concurrent.futures as cf
@@ -54,8 +56,28 @@ import time
 
 import numpy as np
 
-sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
 import pgd_gb300 as pgd  # noqa: E402
+
+
+def oracle_check(graphs, results, cap_edges=20000, count=32):
+    """Compare results[i].totals with the oracle on a sample of the graphs of
+    at most cap_edges pairs, spread evenly over their sizes.  Returns
+    (graphs checked, mismatches)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as ol
+
+    small = [i for i, (s, _) in enumerate(graphs) if len(s) <= cap_edges]
+    small.sort(key=lambda i: len(graphs[i][0]))
+    pick = [small[int(j * (len(small) - 1) / max(1, count - 1))] for j in range(min(count, len(small)))]
+    pick = sorted(set(pick))
+    bad = 0
+    for i in pick:
+        s, d = graphs[i]
+        want = ol.OracleGraph.from_pairs(s, d, dedup=True).run(micro=False).totals()
+        bad += int(not (np.asarray(results[i]) == want).all())
+    return len(pick), bad
 
 
 def log(*a):
@@ -102,7 +124,7 @@ def plain_batch1(ctx, graphs):
     return out, time.perf_counter() - t0
 
 
-def run_batch(args):
+def run_batch(args, emit=True):
     t0 = time.perf_counter()
     graphs, specs = batch_graphs(args.graphs, args.seed)
     pairs = sum(len(s) for s, _ in graphs)
@@ -146,15 +168,23 @@ def run_batch(args):
     for lst in (p_t, p_d, p_b):
         mismatch += sum(int(not (p == res[i].totals).all()) for p, i in zip(lst, idx))
     best_plain = max(plain.values())
+    checked, oracle_bad = oracle_check(graphs, [r.totals for r in res])
     line = {
         "mode": "batch", "graphs": len(graphs), "pairs": pairs, "seconds": best, "graphs_per_s": len(graphs) / best,
         "kernel_ms": float(res[0].kernel_ms) if res else 0.0,
         "plain_graphs": k, "plain_graphs_per_s": plain, "speedup_vs_best_plain": (len(graphs) / best) / best_plain,
-        "mismatches_vs_plain": mismatch,
+        "mismatches_vs_plain": mismatch, "oracle_checked": checked, "oracle_mismatches": oracle_bad,
+        "speedup_vs_single_graph_api": (len(graphs) / best) / max(plain["single_graph_api_default"],
+                                                                  plain["single_graph_api_tuned"]),
+        "speedup_vs_batch_of_one": (len(graphs) / best) / plain["batch_of_one"],
         "thresholds": {"anchor_hub": a, "cache_hub": c, "dense_max": dm},
-        "workload": "4096 graphs, n~U[16,2048], half G(n,p) p~U[0.01,0.5], half BA m~U{2..8}, seed %d" % args.seed,
+        "workload": "%d graphs, n~U[16,2048], half G(n,p) p~U[0.01,0.5], half BA m~U{2..8}, seed %d"
+                    % (len(graphs), args.seed),
     }
-    print(json.dumps(line), flush=True)
+    ctx.close()
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 def serve_requests(count, seed):
@@ -205,7 +235,7 @@ def serve_once(reqs, expect, gaps, workers):
     return stats, wall, mismatch
 
 
-def run_serve(args):
+def run_serve(args, emit=True):
     t0 = time.perf_counter()
     reqs = serve_requests(args.requests, args.seed)
     pairs = sum(len(s) for s, _ in reqs)
@@ -221,6 +251,7 @@ def run_serve(args):
     assert all((x == y).all() for x, y in zip(expect, expect1))
     plain_rates = {"single_graph_api": len(reqs) / plain_s, "batch_of_one": len(reqs) / plain1_s}
     plain_rate = max(plain_rates.values())
+    checked, oracle_bad = oracle_check(reqs, expect)
     log("plain loops: %s graphs/s" % plain_rates)
     # warm-up
     sv = pgd.Server(workers=args.workers)
@@ -228,6 +259,7 @@ def run_serve(args):
         sv.wait(sv.submit(s, d), 60000)
     sv.close()
     rates = [float(r) for r in args.rates.split(",")] if args.rates else [args.rate]
+    lines = []
     for rate in rates:
         rng = np.random.default_rng(args.seed + 1)
         gaps = rng.exponential(1.0 / rate, len(reqs))
@@ -235,13 +267,19 @@ def run_serve(args):
         line = {
             "mode": "serve", "requests": len(reqs), "pairs": pairs, "offered_rate": rate,
             "graphs_per_s": stats["graphs_per_s"], "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"],
-            "mean_ms": stats["mean_ms"], "batches": stats["batches"], "wall_s": wall,
+            "mean_ms": stats["mean_ms"], "queue_p50_ms": stats["queue_p50_ms"], "queue_p99_ms": stats["queue_p99_ms"],
+            "service_p50_ms": stats["service_p50_ms"], "service_p99_ms": stats["service_p99_ms"],
+            "skipped_ahead": stats["skipped_ahead"], "batches": stats["batches"], "wall_s": wall,
             "plain_graphs_per_s": plain_rates, "speedup_vs_best_plain": stats["graphs_per_s"] / plain_rate,
-            "mismatches_vs_plain": mismatch, "workers": args.workers,
+            "mismatches_vs_plain": mismatch, "oracle_checked": checked, "oracle_mismatches": oracle_bad,
+            "workers": args.workers,
             "workload": "Poisson arrivals; m ~ lognormal(median 5000, sigma 1.2, <= 50M); half RMAT, half G(n,p) "
                         "mean degree 16; seed %d" % args.seed,
         }
-        print(json.dumps(line), flush=True)
+        lines.append(line)
+        if emit:
+            print(json.dumps(line), flush=True)
+    return lines
 
 
 RMAT = dict(a=0.57, b=0.19, c=0.19)

@@ -234,18 +234,22 @@ pgd_status pgd_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pair_of
 
 /* ---- request server (no reference counterpart) ---------------------------
  * Continuous batching: submitted graphs queue; `workers` threads, each with
- * its own context and stream, repeatedly admit the oldest pending requests
- * that fit the HBM budget (at most max_batch), decompose them together with
- * pgd_decompose_pairs_batch, and publish each request's global counts.
- * Requests that arrive while a batch runs join the next one; batches of
- * different workers run on the device at the same time.  A request whose own
- * memory estimate exceeds the budget completes with PGD_ENOMEM. */
+ * its own context and stream, repeatedly admit pending requests, oldest
+ * first, that fit the HBM budget (at most max_batch requests and about 2M
+ * pairs per batch), decompose them together with pgd_decompose_pairs_batch,
+ * and publish each request's global counts.  A request that does not fit the
+ * memory left is passed by later, smaller ones until it has waited
+ * max_wait_ms; then it goes next.  Requests that arrive while a batch runs
+ * join the next one; batches of different workers run on the device at the
+ * same time.  A request whose own memory estimate exceeds the budget
+ * completes with PGD_ENOMEM.  Latency quantiles come from fixed log-spaced
+ * histograms (2 % resolution). */
 typedef struct pgd_server pgd_server;
 typedef struct {
     int device;
     int workers;           /* default 2                                     */
     int max_batch;         /* requests per batch, default 4096              */
-    int reserved;
+    int max_wait_ms;       /* age after which a request is no longer passed, default 20 */
     uint64_t hbm_budget;   /* bytes of admitted work; 0 = half of the device's free memory */
 } pgd_server_opts;
 typedef struct {
@@ -253,6 +257,9 @@ typedef struct {
     uint64_t inflight_bytes, peak_bytes;
     double p50_ms, p99_ms, mean_ms;   /* submit -> result latency            */
     double graphs_per_s;              /* completed / (last completion - first submit) */
+    double queue_p50_ms, queue_p99_ms;       /* submit -> admission into a batch */
+    double service_p50_ms, service_p99_ms;   /* admission -> result             */
+    uint64_t skipped_ahead;           /* requests admitted ahead of an older one */
 } pgd_server_stat;
 pgd_status pgd_server_create(const pgd_server_opts *opts, pgd_server **out);
 pgd_status pgd_server_submit(pgd_server *sv, const int32_t *src, const int32_t *dst, int64_t k, int64_t n_min,

@@ -71,14 +71,16 @@ class pgd_counts(ctypes.Structure):
 
 class pgd_server_opts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("workers", ctypes.c_int), ("max_batch", ctypes.c_int),
-                ("reserved", ctypes.c_int), ("hbm_budget", ctypes.c_uint64)]
+                ("max_wait_ms", ctypes.c_int), ("hbm_budget", ctypes.c_uint64)]
 
 
 class pgd_server_stat(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("rejected", ctypes.c_uint64),
                 ("batches", ctypes.c_uint64), ("inflight_bytes", ctypes.c_uint64), ("peak_bytes", ctypes.c_uint64),
                 ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
-                ("graphs_per_s", ctypes.c_double)]
+                ("graphs_per_s", ctypes.c_double), ("queue_p50_ms", ctypes.c_double),
+                ("queue_p99_ms", ctypes.c_double), ("service_p50_ms", ctypes.c_double),
+                ("service_p99_ms", ctypes.c_double), ("skipped_ahead", ctypes.c_uint64)]
 
 
 class pgd_info(ctypes.Structure):
@@ -390,8 +392,8 @@ class Graph:
 class Server:
     """Continuous-batching request server (pgd_server_*)."""
 
-    def __init__(self, device=0, workers=2, max_batch=4096, hbm_budget=0):
-        o = pgd_server_opts(device, workers, max_batch, 0, hbm_budget)
+    def __init__(self, device=0, workers=2, max_batch=4096, hbm_budget=0, max_wait_ms=0):
+        o = pgd_server_opts(device, workers, max_batch, max_wait_ms, hbm_budget)
         h = ctypes.c_void_p()
         st = lib().pgd_server_create(ctypes.byref(o), ctypes.byref(h))
         if st:

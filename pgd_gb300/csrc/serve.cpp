@@ -1,16 +1,22 @@
 // serve.cpp -- continuous-batching request server (no reference counterpart).
 //
 // Requests (one graph each, as host pairs) are queued on submit.  Each
-// worker thread owns a context (its own CUDA stream) and loops: take the
-// oldest pending requests that fit the server's HBM budget (and at most
-// max_batch of them), decompose them together -- one device CSR for the
-// whole set, one pass of the persistent kernels, per-graph sums
-// (pgd_dev_decompose_pairs_batch) -- publish the results, release the
-// memory.  Requests arriving while a batch is on the GPU are admitted by the
+// worker thread owns a context (its own CUDA stream) and loops: take pending
+// requests, oldest first, that fit the server's HBM budget (at most
+// max_batch of them and about kBatchPairs pairs, so that a batch stays short
+// and a request arriving meanwhile soon gets its turn), decompose them
+// together -- one device CSR for the whole set, one pass of the persistent
+// kernels, per-graph sums (pgd_dev_decompose_pairs_batch) -- publish the
+// results, release the memory.  A request that does not fit the memory left
+// is skipped for now and later, smaller requests are admitted ahead of it,
+// until it has waited max_wait_ms: then nothing is admitted past it until it
+// fits.  Requests arriving while a batch is on the GPU are admitted by the
 // next free worker as soon as memory allows, so with two or more workers
 // batches from different workers run on the device at the same time.  A
 // request whose own estimate exceeds the whole budget fails with
-// PGD_ENOMEM; the others are unaffected.
+// PGD_ENOMEM; the others are unaffected.  Latencies are kept in fixed
+// log-spaced histograms (2 % resolution), split into queueing (submit to
+// admission) and service (admission to result).
 #include <string.h>
 
 #include <chrono>
@@ -22,6 +28,7 @@
 #include <unordered_map>
 #include <vector>
 #include <algorithm>
+#include <cmath>
 
 #include "pgd_internal.h"
 
@@ -34,7 +41,7 @@ struct Request {
     std::vector<int32_t> src, dst;
     int64_t n_min = 0;
     uint64_t est_bytes = 0;
-    Clock::time_point t_submit, t_done;
+    Clock::time_point t_submit, t_admit, t_done;
     pgd_counts result{};
     pgd_status status = PGD_OK;
     bool done = false;
@@ -52,6 +59,39 @@ uint64_t estimate_bytes(int64_t pairs, int64_t n) {
     return bytes;
 }
 
+// A batch is closed once it holds this many pairs (it always takes at least
+// one request): long batches make every request that arrives meanwhile wait.
+constexpr int64_t kBatchPairs = 1 << 21;
+constexpr int kDefaultMaxWaitMs = 20;
+
+// Latency histogram with log-spaced buckets: bucket b holds values in
+// [kLo * kStep^b, kLo * kStep^(b+1)) ms, from 1 microsecond to about 10^6 s.
+struct LatencyHist {
+    static constexpr double kLo = 1e-3, kStep = 1.02;
+    static constexpr int kBuckets = 1400;
+    std::vector<uint64_t> count = std::vector<uint64_t>(kBuckets, 0);
+    uint64_t total = 0;
+    double sum = 0;
+    void add(double ms) {
+        int b = ms <= kLo ? 0 : (int)(std::log(ms / kLo) / std::log(kStep));
+        b = std::min(std::max(b, 0), kBuckets - 1);
+        count[(size_t)b]++;
+        total++;
+        sum += ms;
+    }
+    // upper edge of the bucket holding the f-quantile
+    double quantile(double f) const {
+        if (!total) return 0;
+        const uint64_t want = std::min<uint64_t>(total, (uint64_t)(f * (double)total) + 1);
+        uint64_t seen = 0;
+        for (int b = 0; b < kBuckets; b++) {
+            seen += count[(size_t)b];
+            if (seen >= want) return kLo * std::pow(kStep, b + 1);
+        }
+        return kLo * std::pow(kStep, kBuckets);
+    }
+};
+
 }  // namespace
 
 struct pgd_server {
@@ -63,8 +103,8 @@ struct pgd_server {
     std::deque<Request *> pending;
     std::unordered_map<uint64_t, Request *> requests;
     uint64_t next_ticket = 1, inflight = 0, peak = 0;
-    uint64_t submitted = 0, completed = 0, rejected = 0, batches = 0;
-    std::vector<double> latencies_ms;
+    uint64_t submitted = 0, completed = 0, rejected = 0, batches = 0, skipped_ahead = 0;
+    LatencyHist lat, lat_queue, lat_service;
     Clock::time_point t_first{}, t_last{};
     bool have_first = false;
     bool stop = false;
@@ -82,21 +122,36 @@ struct pgd_server {
                 std::unique_lock<std::mutex> lock(mu);
                 cv_work.wait(lock, [&] { return stop || !pending.empty(); });
                 if (pending.empty() && stop) return;
-                // admit the oldest requests that fit; refuse what can never fit
-                while (!pending.empty() && (int)batch.size() < opts.max_batch) {
-                    Request *r = pending.front();
+                // admit pending requests that fit, oldest first; skip one that
+                // does not fit yet unless it has waited max_wait_ms; refuse what
+                // can never fit
+                const Clock::time_point now = Clock::now();
+                const auto max_wait = std::chrono::milliseconds(opts.max_wait_ms);
+                int64_t pairs = 0;
+                bool skipped = false;
+                for (auto it = pending.begin();
+                     it != pending.end() && (int)batch.size() < opts.max_batch && pairs < kBatchPairs;) {
+                    Request *r = *it;
                     if (r->est_bytes > opts.hbm_budget) {
-                        pending.pop_front();
+                        it = pending.erase(it);
                         r->status = PGD_ENOMEM;
                         r->done = true;
-                        r->t_done = Clock::now();
+                        r->t_done = now;
                         rejected++;
                         cv_done.notify_all();
                         continue;
                     }
-                    if (inflight + bytes + r->est_bytes > opts.hbm_budget) break;
-                    pending.pop_front();
+                    if (inflight + bytes + r->est_bytes > opts.hbm_budget) {
+                        if (now - r->t_submit >= max_wait) break;   // it goes next, nothing passes it
+                        skipped = true;
+                        ++it;
+                        continue;
+                    }
+                    if (skipped) skipped_ahead++;
+                    it = pending.erase(it);
                     bytes += r->est_bytes;
+                    pairs += (int64_t)r->src.size();
+                    r->t_admit = now;
                     batch.push_back(r);
                 }
                 if (batch.empty()) {
@@ -135,7 +190,9 @@ struct pgd_server {
                     r->dst.clear();
                     r->dst.shrink_to_fit();
                     completed++;
-                    latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
+                    lat.add(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
+                    lat_queue.add(std::chrono::duration<double, std::milli>(r->t_admit - r->t_submit).count());
+                    lat_service.add(std::chrono::duration<double, std::milli>(now - r->t_admit).count());
                 }
                 t_last = now;
                 inflight -= bytes;
@@ -153,6 +210,7 @@ extern "C" pgd_status pgd_server_create(const pgd_server_opts *opts, pgd_server 
     if (opts) sv->opts = *opts;
     if (sv->opts.workers <= 0) sv->opts.workers = 2;
     if (sv->opts.max_batch <= 0) sv->opts.max_batch = 4096;
+    if (sv->opts.max_wait_ms <= 0) sv->opts.max_wait_ms = kDefaultMaxWaitMs;
     for (int i = 0; i < sv->opts.workers; i++) {
         pgd_opts o{};
         o.device = sv->opts.device;
@@ -244,15 +302,15 @@ extern "C" pgd_status pgd_server_stats(pgd_server *sv, pgd_server_stat *st) {
     st->batches = sv->batches;
     st->inflight_bytes = sv->inflight;
     st->peak_bytes = sv->peak;
-    std::vector<double> l = sv->latencies_ms;
-    if (!l.empty()) {
-        std::sort(l.begin(), l.end());
-        auto q = [&](double f) { return l[std::min(l.size() - 1, (size_t)(f * (double)(l.size() - 1) + 0.5))]; };
-        st->p50_ms = q(0.50);
-        st->p99_ms = q(0.99);
-        double s = 0;
-        for (double x : l) s += x;
-        st->mean_ms = s / (double)l.size();
+    st->skipped_ahead = sv->skipped_ahead;
+    if (sv->lat.total) {
+        st->p50_ms = sv->lat.quantile(0.50);
+        st->p99_ms = sv->lat.quantile(0.99);
+        st->mean_ms = sv->lat.sum / (double)sv->lat.total;
+        st->queue_p50_ms = sv->lat_queue.quantile(0.50);
+        st->queue_p99_ms = sv->lat_queue.quantile(0.99);
+        st->service_p50_ms = sv->lat_service.quantile(0.50);
+        st->service_p99_ms = sv->lat_service.quantile(0.99);
         const double span = std::chrono::duration<double>(sv->t_last - sv->t_first).count();
         st->graphs_per_s = span > 0 ? (double)sv->completed / span : 0;
     }

@@ -103,3 +103,24 @@ def test_server_poll_and_timeout():
         assert got is not None and got[0] == 0
         assert (got[1].totals == oracle_totals(s, d)).all()
     sv.close()
+
+
+def test_server_admits_small_requests_past_a_large_one():
+    """A request that does not fit the memory left is passed by later, smaller
+    ones (until it has waited max_wait_ms); every result stays exact."""
+    big1 = pgd.rmat(16, 16, seed=11)
+    big2 = pgd.rmat(16, 16, seed=12)
+    smalls = [pgd.erdos_renyi(40, 0.3, seed=20 + i) for i in range(40)]
+    # two large requests cannot be in flight together under this budget
+    sv = pgd.Server(workers=2, hbm_budget=300 << 20, max_wait_ms=60000)
+    t1 = sv.submit(*big1)
+    t2 = sv.submit(*big2)
+    ts = [sv.submit(*g) for g in smalls]
+    for tk, g in zip([t1, t2] + ts, [big1, big2] + smalls):
+        st, r = sv.wait(tk, 120000)
+        assert st == 0 and (r.totals == oracle_totals(*g)).all()
+    s = sv.stats()
+    assert s["completed"] == 42 and s["skipped_ahead"] >= 1
+    assert s["queue_p50_ms"] <= s["queue_p99_ms"] and s["service_p50_ms"] <= s["service_p99_ms"]
+    assert s["p99_ms"] >= s["p50_ms"] > 0
+    sv.close()
