@@ -306,7 +306,9 @@ def run_profile(args):
     for _ in range(args.reps):
         res = g.decompose(micro=True)
         print(json.dumps({"mode": "profile", "scale": args.scale, "order": args.order, "n": int(res.n),
-                          "m": int(res.m), "kernel_ms": float(res.kernel_ms)}), flush=True)
+                          "m": int(res.m), "kernel_ms": float(res.kernel_ms), "hub_ms": float(res.hub_ms)}),
+              flush=True)
+    g.micro()   # the per-edge ids of the output rows (k_micro_ids)
 
 
 def run_small(args):
