@@ -66,6 +66,8 @@ constexpr int kMaxChunks = 8;            // ... but an anchor is split into at m
 constexpr int kMaxDynSmem = 156 * 1024;  // k_hub dynamic shared memory: bitmap, then the W histogram
 constexpr int kMaxTslotSmem = 200 * 1024;  // k_tslot_hub dynamic shared memory: rank bitmap
 constexpr int kTHigh = 4096;             // T members of rank >= kRankBits listed per warp (beyond: search N(q))
+constexpr int kTWin = 1 << 18;           // T members of rank in [kRankBits, kTWin) also marked in a per-warp
+                                         // global bitmap (30 KB), so membership there is one load
 constexpr int kRankBits = 16384;         // T members of degree rank below this are marked in a per-warp bitmap;
                                          // vertices of rank below this get a rank-bitmap row of N+(x)
 
@@ -185,14 +187,18 @@ __global__ void k_gather_rank(const int32_t *adjp, const int32_t *vrank, int64_t
         out[i] = vrank[adjp[i]];
 }
 
-// Rank-bitmap rows: the vertex of rank r < top_r gets a row of (r >> 5) + 1
-// words with bit r_y set for every y in N+(x) (all of rank < r).  Rows are
-// stored back to back in rank order; row r starts at word
-// sum_{r' < r} ((r' >> 5) + 1) = (a + 1) * (16 a + b) for r = 32 a + b.
+// Rank-bitmap rows: the vertex of rank r < top_r gets a row of (r >> 6) + 1
+// 64-bit words (2 ((r >> 6) + 1) 32-bit words) with bit r_y set for every y in
+// N+(x) (all of rank < r).  Rows are stored back to back in rank order, each
+// 8-byte aligned: row r starts at 64-bit word sum_{r' < r} ((r' >> 6) + 1) =
+// (a + 1) * (32 a + b) for r = 64 a + b; returned here in 32-bit words.
 __host__ __device__ __forceinline__ int64_t top_row_base(int64_t r) {
-    const int64_t a = r >> 5, b = r & 31;
-    return (a + 1) * (16 * a + b);
+    const int64_t a = r >> 6, b = r & 63;
+    return 2 * (a + 1) * (32 * a + b);
 }
+
+// 32-bit words of row r
+__host__ __device__ __forceinline__ int top_row_words(int32_t r) { return 2 * ((r >> 6) + 1); }
 
 __global__ void k_top_rows(const int64_t *offp, const int32_t *adjp_rank, const int32_t *vrank, int64_t n, int top_r,
                            uint32_t *rows) {
@@ -227,7 +233,7 @@ __global__ void k_slot_fill(const int32_t *adj, const int32_t *vrank, const int3
                             int64_t nnz, int top_r, int4 *slot) {
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nnz; j += (int64_t)gridDim.x * blockDim.x) {
         const int32_t w = adj[j], r = vrank[w];
-        const bool row = r < top_r && (r >> 5) + 1 < (int)(offp[w + 1] - offp[w]);
+        const bool row = r < top_r && top_row_words(r) < (int)(offp[w + 1] - offp[w]);
         slot[j] = make_int4(w, (int)((uint32_t)r | (row ? 0x80000000u : 0u)), hubid[w], 0);
     }
 }
@@ -493,6 +499,8 @@ struct HubArgs {
     unsigned long long *next;
     int4 *slot_out;           // k_tslot_hub: slot records whose t it writes
     int32_t *thigh;           // k_hub: per-warp lists of T's high-rank members (kTHigh each)
+    uint32_t *twin;           // k_hub: per-warp bitmaps of T's members of rank in [kRankBits, kRankBits + 32 twin_words)
+    int32_t twin_words;
 };
 
 // |{r in L[0..len) : r in N(p)}| for a list of ranks, warp-cooperative,
@@ -508,12 +516,16 @@ __device__ __forceinline__ unsigned count_bits(const RankBits &bm, const int32_t
     return c;
 }
 
-// sum over words of popc(row & Rw), warp-cooperative
+// sum over the row's words of popc(row & Rw), warp-cooperative, 64 bits per
+// load (rows and the T bitmap are 8-byte aligned; words is even)
 __device__ __forceinline__ unsigned row_and_count(const uint32_t *row, const uint32_t *Rw, int words, int lane) {
+    const unsigned long long *r64 = (const unsigned long long *)row;
+    const unsigned long long *t64 = (const unsigned long long *)Rw;
+    const int w64 = words >> 1;
     unsigned c = 0;
     int i = lane;
-    for (; i + 32 < words; i += 64) c += __popc(__ldg(row + i) & Rw[i]) + __popc(__ldg(row + i + 32) & Rw[i + 32]);
-    if (i < words) c += __popc(__ldg(row + i) & Rw[i]);
+    for (; i + 32 < w64; i += 64) c += __popcll(__ldg(r64 + i) & t64[i]) + __popcll(__ldg(r64 + i + 32) & t64[i + 32]);
+    if (i < w64) c += __popcll(__ldg(r64 + i) & t64[i]);
     return c;
 }
 
@@ -528,10 +540,20 @@ struct THigh {
     int count;       // -1: more than kTHigh, search N(q) instead
 };
 
-__device__ __forceinline__ bool in_t(const uint32_t *Rw, const RankBits &bm, const int32_t *Nq, int dq, int32_t y,
-                                     int32_t ry, const THigh &th) {
+// T's members of rank in [kRankBits, kRankBits + 32 twin_words), marked by
+// the warp in pass 1 in its global bitmap (written by atomics, so read past
+// L1).  Addressed from the kernel parameters so that no register holds it.
+__device__ __forceinline__ uint32_t *twin_of(const HubArgs &A) {
+    return A.twin + ((int64_t)blockIdx.x * kHubWarps + (threadIdx.x >> 5)) * A.twin_words;
+}
+
+// y (rank ry, id at *yp, loaded only when needed) in T?
+__device__ __forceinline__ bool in_t(const uint32_t *Rw, const HubArgs &A, const RankBits &bm, const int32_t *Nq,
+                                     int dq, const int32_t *yp, int32_t ry, const THigh &th) {
     if (ry < kRankBits) return (Rw[ry >> 5] >> (ry & 31)) & 1u;
+    if (ry < kRankBits + 32 * A.twin_words) return (__ldcg(twin_of(A) + ((ry - kRankBits) >> 5)) >> (ry & 31)) & 1u;
     if (!bm.test(ry)) return false;
+    const int32_t y = __ldg(yp);
     return th.count >= 0 ? pgd_contains(th.ids, th.count, y) : pgd_contains(Nq, dq, y);
 }
 
@@ -539,8 +561,9 @@ __device__ __forceinline__ int64_t rec_off(const int4 &ra) { return (int64_t)(((
 __device__ __forceinline__ int64_t rec_offp(const int4 &ra) { return (int64_t)(((uint64_t)(uint32_t)ra.w << 32) | (uint32_t)ra.z); }
 
 // What pass 2 scans for neighbour w of q (slot record sr): for w in T, N+(w)
-// as a rank-bitmap row (kind 2, from the rank alone) or as a list (kind 1);
-// for a non-hub w outside N(p), N(w) (kind 0); nothing otherwise (len 0).
+// as a rank-bitmap row (kind 2, from the rank alone) or as a list of ranks
+// (kind 1, with the ids beside them for the rare test that needs one); for a
+// non-hub w outside N(p), N(w)'s ranks (kind 0); nothing otherwise (len 0).
 // Lists need w's offsets: one 32-byte vertex record.
 __device__ __forceinline__ void plan_entry(const DevGraph &G, bool inT, const int4 &sr, int &len, int &kind,
                                            const int32_t *&list, const int32_t *&rlist) {
@@ -549,15 +572,15 @@ __device__ __forceinline__ void plan_entry(const DevGraph &G, bool inT, const in
         const int32_t r = sr.y & 0x7fffffff;
         if (sr.y < 0) {
             kind = 2;
-            len = (r >> 5) + 1;
+            len = top_row_words(r);
             list = (const int32_t *)(G.toprows + top_row_base(r));
         } else {
             const int4 ra = __ldg(G.vrec + 2 * (int64_t)w), rb = __ldg(G.vrec + 2 * (int64_t)w + 1);
             const int64_t o = rec_offp(ra);
             kind = 1;
             len = rb.y;
-            list = G.adjp + o;
-            rlist = G.adjp_rank + o;
+            list = G.adjp_rank + o;
+            rlist = G.adjp + o;
         }
     } else if (sr.z < 0) {
         const int4 ra = __ldg(G.vrec + 2 * (int64_t)w), rb = __ldg(G.vrec + 2 * (int64_t)w + 1);
@@ -795,6 +818,8 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                             sumtq += (uint32_t)sr.w;
                             const int32_t r = sr.y & 0x7fffffff;
                             if (r < kRankBits) atomicOr(Rw + (r >> 5), 1u << (r & 31));
+                            else if (r < kRankBits + 32 * A.twin_words)
+                                atomicOr(twin_of(A) + ((r - kRankBits) >> 5), 1u << (r & 31));
                             hi = r >= kRankBits;
                         } else {
                             const int32_t h = sr.z;
@@ -851,11 +876,11 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                     } else {
                         int i = lane;
                         for (; i + 32 < ln; i += 64) {
-                            const int32_t y0 = __ldg(L + i), y1 = __ldg(L + i + 32);
-                            const int32_t r0 = __ldg(LR + i), r1 = __ldg(LR + i + 32);
-                            k4 += (in_t(Rw, bm, Nq, dq, y0, r0, th) ? 1 : 0) + (in_t(Rw, bm, Nq, dq, y1, r1, th) ? 1 : 0);
+                            const int32_t r0 = __ldg(L + i), r1 = __ldg(L + i + 32);
+                            k4 += (in_t(Rw, A, bm, Nq, dq, LR + i, r0, th) ? 1 : 0) +
+                                  (in_t(Rw, A, bm, Nq, dq, LR + i + 32, r1, th) ? 1 : 0);
                         }
-                        for (; i < ln; i += 32) k4 += in_t(Rw, bm, Nq, dq, __ldg(L + i), __ldg(LR + i), th) ? 1 : 0;
+                        for (; i < ln; i += 32) k4 += in_t(Rw, A, bm, Nq, dq, LR + i, __ldg(L + i), th) ? 1 : 0;
                     }
                 }
                 // short lists: flattened over the warp
@@ -876,17 +901,15 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                     const int idxB = itB - __shfl_sync(0xffffffffu, excl, ownB);
                     const bool vA = itA < total, vB = itB < total;
                     const int32_t xA = vA ? __ldg(olA + idxA) : 0, xB = vB ? __ldg(olB + idxB) : 0;
-                    const int32_t rA = (vA && okA == 1) ? __ldg(orA + idxA) : 0;
-                    const int32_t rB = (vB && okB == 1) ? __ldg(orB + idxB) : 0;
                     if (vA) {
                         if (okA == 0) sumW += bm.test(xA);
                         else if (okA == 2) k4 += __popc((uint32_t)xA & Rw[idxA]);
-                        else k4 += in_t(Rw, bm, Nq, dq, xA, rA, th) ? 1 : 0;
+                        else k4 += in_t(Rw, A, bm, Nq, dq, orA + idxA, xA, th) ? 1 : 0;
                     }
                     if (vB) {
                         if (okB == 0) sumW += bm.test(xB);
                         else if (okB == 2) k4 += __popc((uint32_t)xB & Rw[idxB]);
-                        else k4 += in_t(Rw, bm, Nq, dq, xB, rB, th) ? 1 : 0;
+                        else k4 += in_t(Rw, A, bm, Nq, dq, orB + idxB, xB, th) ? 1 : 0;
                     }
                 }
             }
@@ -898,6 +921,19 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
             edge_epilogue_d(G, acc, cur_g, e, dp, dq, t, k4, (unsigned long long)c4, lane);
             __syncwarp();
             for (int i = lane; i < kRankBits / 32; i += 32) Rw[i] = 0;
+            if (A.twin_words) {
+                // clear the window words of T's listed high-rank members, or all of
+                // it when the list overflowed
+                uint32_t *twp = twin_of(A);
+                if (nhigh >= 0) {
+                    for (int i = lane; i < nhigh; i += 32) {
+                        const int32_t r = G.vrank[th.ids[i]];
+                        if (r < kRankBits + 32 * A.twin_words) twp[(r - kRankBits) >> 5] = 0;
+                    }
+                } else {
+                    for (int i = lane; i < A.twin_words; i += 32) twp[i] = 0;
+                }
+            }
             __syncwarp();
             kc = kn;
             rc = rn;
@@ -1639,6 +1675,9 @@ struct DenseView {
 // remaining shared memory holds; per-CTA global slices for the rest.  Fills
 // the layout fields of H and returns the dynamic shared memory size.
 static size_t hub_layout(int64_t n, int32_t nhubs, int32_t nwide, int32_t max_degree, HubArgs *H) {
+    H->thigh = nullptr;
+    H->twin = nullptr;
+    H->twin_words = 0;
     H->nwords = (n + 31) / 32;
     H->nhubs = nhubs;
     H->nwide = nwide;
@@ -1754,6 +1793,14 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
             if ((st = tg.alloc(&ghist, (size_t)nsm * H.hstride * 4))) return st;
         }
         if ((st = tg.alloc(&thigh, (size_t)nsm * kHubWarps * kTHigh * sizeof(int32_t)))) return st;
+        if (G.n > kRankBits) {
+            // per-warp window bitmaps over ranks [kRankBits, min(n, kTWin)), zero at the start
+            const int64_t lim = std::min<int64_t>(G.n, kTWin);
+            H.twin_words = (int32_t)((lim - kRankBits + 31) / 32);
+            const size_t bytes = (size_t)nsm * kHubWarps * H.twin_words * sizeof(uint32_t);
+            if ((st = tg.alloc(&H.twin, bytes))) return st;
+            PGD_CUDA(ctx, cudaMemsetAsync(H.twin, 0, bytes, s));
+        }
         PGD_CUDA(ctx, cudaFuncSetAttribute(k_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         H.G = G;
         H.hpos = posv;
