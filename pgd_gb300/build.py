@@ -37,8 +37,8 @@ def cuda_home():
 CUDA = cuda_home()
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 
-CU_SOURCES = ["graph_build.cu", "decompose.cu"]
-CPP_SOURCES = ["api.cpp", "reader.cpp", "closing.cpp", "gen.cpp", "serve.cpp"]
+CU_SOURCES = ["graph_build.cu", "decompose.cu", "ingest.cu"]
+CPP_SOURCES = ["api.cpp", "closing.cpp", "gen.cpp", "serve.cpp"]
 CLI_SOURCES = ["graphlet_core.cpp", "pgd_cli.cpp"]
 
 

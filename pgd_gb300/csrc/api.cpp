@@ -9,7 +9,6 @@
 #include <vector>
 
 #include "pgd_internal.h"
-#include "pgd_reader.h"
 
 // ---------------------------------------------------------------------------
 // errors and memory
@@ -209,18 +208,14 @@ extern "C" pgd_status pgd_graph_from_csr(pgd_ctx *ctx, const int64_t *off, const
 
 extern "C" pgd_status pgd_graph_from_file(pgd_ctx *ctx, const char *path, pgd_graph **out) {
     if (!ctx || !out || !path) return pgd_fail(ctx, PGD_EINVAL, "bad arguments");
-    ReadResult r;
-    if (!pgd_read_graph_file(path, r)) {
-        bool missing = r.error.rfind("file not found", 0) == 0;
-        return pgd_fail(ctx, missing ? PGD_EIO : PGD_EINVAL, r.error);
-    }
-    pgd_status st = pgd_graph_from_edges(ctx, r.src.data(), r.dst.data(), (int64_t)r.src.size(), 0,
-                                         r.is_mtx ? 0u : PGD_EDGES_DEDUP, out);
-    if (st == PGD_OK) (*out)->self_loops = r.self_loops;
-    if (st == PGD_EINVAL && r.is_mtx && ctx->err.find("repeated pair") != std::string::npos)
+    cudaSetDevice(ctx->device);
+    pgd_graph *g = new_graph(ctx);
+    bool mtx = false;
+    pgd_status st = pgd_build_from_file(g, path, &mtx);
+    if (st == PGD_EINVAL && mtx && ctx->err.find("repeated pair") != std::string::npos)
         ctx->err = "mtx file lists an edge twice; the reference does not deduplicate mtx input and its counts "
                    "are undefined for multigraphs";
-    return st;
+    return finish_new(g, st, out);
 }
 
 extern "C" pgd_status pgd_graph_info(const pgd_graph *g, pgd_info *info) {

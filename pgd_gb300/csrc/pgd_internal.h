@@ -113,6 +113,8 @@ pgd_status pgd_build_from_pairs(pgd_graph *g, const int32_t *h_src, const int32_
 pgd_status pgd_build_from_device_pairs(pgd_graph *g, const int32_t *d_src, const int32_t *d_dst, int64_t k,
                                        int64_t n_min, bool dedup);
 pgd_status pgd_build_from_csr(pgd_graph *g, const int64_t *h_off, const int32_t *h_adj, int64_t n);
+// ingest.cu: a graph file parsed on the device with the reference reader's rules
+pgd_status pgd_build_from_file(pgd_graph *g, const char *path, bool *mtx);
 pgd_status pgd_dev_preprocess(pgd_graph *g, int neigh_kind, int s2l);
 pgd_status pgd_dev_cores(pgd_graph *g);
 pgd_status pgd_dev_assortativity(pgd_graph *g, double *r);

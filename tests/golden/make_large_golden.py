@@ -16,7 +16,7 @@ Writes, per graph, tests/golden/<name>.json:
   and 256 rows in full (the first 64 positions and 192 seeded random ones),
   so that a digest mismatch can be localised.
 
-Run:  python tests/golden/make_large_golden.py [rmat20_kcore] [rgg20_kcore]
+Run:  python tests/golden/make_large_golden.py [rmat20_kcore] [rgg20_kcore] [rgg24_kcore]
 """
 import hashlib
 import json
@@ -43,6 +43,7 @@ CASES = {
     "rmat20_kcore": {"kind": "rmat", "scale": 20, "edge_factor": 16, "a": 0.57, "b": 0.19, "c": 0.19, "seed": 1,
                      "order": "kcore"},
     "rgg20_kcore": {"kind": "rgg3d", "n": 1 << 20, "mean_degree": 24, "seed": 1, "order": "kcore"},
+    "rgg24_kcore": {"kind": "rgg3d", "n": 1 << 24, "mean_degree": 24, "seed": 1, "order": "kcore"},
 }
 
 

@@ -83,3 +83,38 @@ def brute_force_counts(n, edges):
     out["total_2_1edge"] = m
     out["total_2_indep"] = n * (n - 1) // 2 - m
     return out
+
+
+# Reader quirks: files whose ids, delimiters, line endings, comments and
+# missing fields exercise the reference reader's rules (graphlet_core.cpp:
+# 196-241 tokens, 291-457 edge lists, 459-522 mtx).  Each was run through the
+# reference's own ./pgd (built from source) without a crash or a hang.
+READER_QUIRKS = {
+    "crlf.txt": "1 2\r\n2 3\r\n3 1\r\n3 4\r\n",
+    "three_spaces.txt": "1   2\n2   3\n3   1\n1   4\n",
+    "banner.txt": "%%MatrixMarket matrix coordinate pattern symmetric\n% c\n4 4 3\n1 2\n2 3\n3 1\n",
+    "comments_between.txt": "1 2\n\n# mid\n2 3\n% x\n3 1\n\n",
+    "no_final_newline.txt": "1 2\n2 3\n3 1",
+    "missing_first_id.txt": "0 1\n 2\n1 2\n2 0\n3 4\n",
+    "single_token.txt": "1 2\n5\n2 3\n3 1\n",
+    "trailing_junk.csv": "1,2\n2,3\n3,1x\n4,1\n",
+    "leading_spaces.txt": "  1 2\n2 3\n3 1\n",
+    "zero_late.edges": "1 2\n2 3\n0 1\n3 0\n",
+    "empty_first_line.txt": "% c\n\n1 2\n2 3\n3 1\n",
+    "header_and_empty_field.csv": "a,b\n1,2\n2,3\n,4\n3,1\n",
+    "empty_middle_field.tab": "1\t2\t9\n2\t3\t9\n3\t\t9\n3\t1\t9\n",
+    "comments.mtx": "%%MatrixMarket matrix coordinate pattern symmetric\n% comment\n5 5 4\n2 1\n3 2\n% mid\n3 1\n5 4\n",
+    "zero_size_line.mtx": "0 0 0\n1 2\n",
+    "missing_second_id.mtx": "6 6 4\n3 2\n5 \n6 1\n4 2\n",
+    "single_id.mtx": "6 6 4\n2 3\n5\n6 1\n",
+    "crlf.mtx": "3 3 2\r\n2 1\r\n3 2\r\n",
+    "self_loop_no_final_newline.mtx": "3 3 3\n1 1\n2 1\n3 2",
+}
+
+# Files on which the reference indexes its relabel table out of bounds (an id
+# carried over from the previous line, already relabelled, then decremented
+# to -1): undefined there, refused with PGD_EINVAL here and by the oracle.
+READER_REFUSED = {
+    "carried_id_below_zero.txt": "1 2\n 3\n2 3\n4 5\n3 1\n",
+    "negative_id.txt": "1 2\n2 -3\n",
+}

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import oracle_lib as ol
-from helpers import (bign_pairs, brute_force_counts, load_npz, load_toys, mtx_pairs, rows_digest)
+from helpers import (READER_QUIRKS, bign_pairs, brute_force_counts, load_npz, load_toys, mtx_pairs, rows_digest)
 
 SYNTH = ["er250", "rmat12", "ba2000", "er1500"]
 ORDERS = [("deg", False), ("kcore", False), ("natural", False), ("deg", True)]
@@ -182,6 +182,20 @@ EDGE_LIST_CASES = {
 def test_reader_rules_vs_reference(tmp_path, fname):
     p = tmp_path / fname
     p.write_text(EDGE_LIST_CASES[fname])
+    r = ol.RefGraph.from_file(str(p)).run(micro=True)
+    g = ol.OracleGraph.from_file(str(p)).run(micro=True)
+    assert (g.n, g.m) == (r.n, r.m)
+    assert (g.totals() == r.totals()).all()
+    a, b, c = g.micro()
+    x, y, z = r.micro()
+    assert (a == x).all() and (b == y).all() and (c == z).all()
+
+
+@needs_ref
+@pytest.mark.parametrize("fname", sorted(READER_QUIRKS))
+def test_reader_quirks_vs_reference(tmp_path, fname):
+    p = tmp_path / fname
+    p.write_bytes(READER_QUIRKS[fname].encode())
     r = ol.RefGraph.from_file(str(p)).run(micro=True)
     g = ol.OracleGraph.from_file(str(p)).run(micro=True)
     assert (g.n, g.m) == (r.n, r.m)
