@@ -154,6 +154,30 @@ def profile_figures():
     return out
 
 
+def write_mtx(path, ev, eu):
+    """A simple graph (each undirected edge once, 0-based ids) as the
+    reference's benchmark file: an mtx file, 1-based, larger id first, with
+    fixed-width right-aligned fields (the reader skips the leading blanks)."""
+    ev = np.asarray(ev, np.int64)
+    eu = np.asarray(eu, np.int64)
+    lo = np.minimum(ev, eu) + 1
+    hi = np.maximum(ev, eu) + 1
+    n = int(hi.max())
+    width = len(str(n))
+    rows = np.full((len(lo), 2 * width + 2), ord(" "), np.uint8)
+    for col, vals in ((0, hi), (width + 1, lo)):
+        v = vals.copy()
+        for k in range(width - 1, -1, -1):
+            digit = (v % 10).astype(np.uint8) + ord("0")
+            rows[:, col + k] = np.where((v > 0) | (k == width - 1), digit, ord(" "))
+            v //= 10
+    rows[:, -1] = ord("\n")
+    with open(path, "wb") as f:
+        f.write(b"%%%%MatrixMarket matrix coordinate pattern symmetric\n%d %d %d\n" % (n, n, len(lo)))
+        f.write(rows.tobytes())
+    return os.path.getsize(path)
+
+
 def golden_totals(scale, order):
     """The oracle's full-run totals of this workload, where committed."""
     p = os.path.join(GOLDEN, "rmat%d_%s.json" % (scale, order))
@@ -418,6 +442,48 @@ def main():
                "d2h_bytes_per_step": int(m * (pgd.NMICRO * 8 + 12) + (pgd.NTOTALS + pgd.NSUMS) * 8)}
         log("rank %d: e2e %.1f ms/step" % (rank, e2e_ms))
 
+    # ---- end to end from the graph file (device ingest) --------------------
+    # the reference's benchmark input, an mtx file of the same graph, read by
+    # pgd_graph_from_file (one copy of the file's bytes, parsing on the device)
+    e2e_file = None
+    if not args.no_e2e and rank == 0:
+        import tempfile
+
+        tdir = tempfile.mkdtemp(prefix="pgd_bench_")
+        path = os.path.join(tdir, "rmat%d.mtx" % args.scale)
+        fbytes = write_mtx(path, ev, eu)
+
+        def file_step():
+            gf = ctx.graph_from_file(path)
+            gf.preprocess("deg")
+            gf.compute_cores()
+            gf.sort_edges(args.order)
+            res = gf.decompose(micro=True)
+            st = pgd.lib().pgd_get_micro(gf.h, pgd._ptr(h_s1), pgd._ptr(h_d1), pgd._ptr(h_cols))
+            assert st == 0
+            gf.destroy()
+            return res
+
+        file_step()
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.e2e_steps):
+            res = file_step()
+            assert (res.totals == ref_totals).all()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        fms = f0.elapsed_time(f1) / args.e2e_steps
+        os.remove(path)
+        os.rmdir(tdir)
+        e2e_file = {"value": m / (fms / 1000.0), "unit": UNIT, "ms_per_step": fms, "file_bytes": int(fbytes),
+                    "h2d_bytes_per_step": int(fbytes),
+                    "d2h_bytes_per_step": int(m * (pgd.NMICRO * 8 + 16) + (pgd.NTOTALS + pgd.NSUMS) * 8),
+                    "what": "mtx file -> counts: file read, one copy of its bytes, device parsing with the reader's "
+                            "rules, CSR build, neighbour order, k-core, sort, decomposition, per-edge rows to host"}
+        log("rank %d: e2e from the %.0f MB mtx file %.1f ms/step" % (rank, fbytes / 1e6, fms))
+
     # ---- CPU baseline (rank 0, N = 1) ---------------------------------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -468,7 +534,7 @@ def main():
             "config": workload_config(args.scale, args.order, n, m), "roofline": roofline,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
             "totals": {k_: int(v) for k_, v in zip(pgd.TOTAL_NAMES, ref_totals)},
-            "batched": batched, "served": served,
+            "e2e_file": e2e_file, "batched": batched, "served": served,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
