@@ -15,8 +15,12 @@ ordering, k-core, decomposition and the copy of all per-edge rows back.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
-With N > 1 (torchrun) every rank decomposes its own copy of the workload
-(independent graphs, no collective on the data path): weak scaling.
+With N > 1 (torchrun) the graph's ordered edge list is cut into N spans of
+about equal estimated work (pgd_gb300/shard.py): every rank holds the whole
+graph, decomposes its span, and the 15 partial sums are added with one NCCL
+all-reduce before the totals are closed -- strong scaling (`--mode shard`,
+the default).  `--mode replicas` instead decomposes an independent copy per
+rank (no collective on the data path): weak scaling.
 """
 import argparse
 import json
@@ -120,15 +124,17 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def algorithmic_bytes(ev, eu, n, micro=True, anchor_hub=None):
+def algorithmic_bytes(ev, eu, n, micro=True, anchor_hub=None, ids=None):
     """Bytes an edge-centric decomposition must stream: per edge both
     endpoint lists plus the 2-hop lists of the cheaper endpoint, 4 B per
     adjacency entry, plus 64 B of per-edge output (micro).  With anchor_hub,
     only the edges whose anchor (the endpoint of higher (degree, id)) has at
-    least that degree: the units of the hub-anchored kernel.  Returns
-    (bytes, edges counted)."""
+    least that degree: the units of the hub-anchored kernel.  With ids, only
+    those edges (a rank's span).  Returns (bytes, edges counted)."""
     deg = np.bincount(ev, minlength=n) + np.bincount(eu, minlength=n)
     vol2 = np.bincount(ev, weights=deg[eu], minlength=n) + np.bincount(eu, weights=deg[ev], minlength=n)
+    if ids is not None:
+        ev, eu = ev[ids], eu[ids]
     sel = slice(None)
     if anchor_hub is not None:
         dv, du = deg[ev], deg[eu]
@@ -266,6 +272,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mode", default="shard", choices=["shard", "replicas"],
+                    help="N > 1: one graph cut into spans (strong scaling) or a copy per rank (weak)")
     ap.add_argument("--scale", type=int, default=20)
     ap.add_argument("--order", default="kcore")
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -324,8 +332,30 @@ def main():
     n, m = info.n, info.m
     log("rank %d: graph n=%d m=%d dmax=%d K=%d built in %.2fs" % (rank, n, m, info.max_degree, K, time.time() - t0))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    sharded = world > 1 and args.mode == "shard"
+    span_ids = None
+    if sharded:
+        from pgd_gb300 import shard
+
+        g.sort_edges(args.order)
+        sev, seu, sids = g.edges()
+        sdeg = np.bincount(sev, minlength=n) + np.bincount(seu, minlength=n)
+        lo, hi = shard.edge_spans(shard.edge_cost(sev, seu, sdeg, sids, ctx.thresholds()[1]), world)[rank]
+        span_ids = sids[lo:hi].astype(np.int64)
+        log("rank %d: span [%d, %d) of %d ordered edges" % (rank, lo, hi, m))
+
+    def decompose_span(gr):
+        """This rank's span (natural order keeps E_ordered's), then the one
+        exchange: the wrapping sum of the 15 partials; totals closed here."""
+        gr.sort_edges_sample(span_ids, "natural", s2l=True)
+        r = gr.decompose(micro=True)
+        r.sums = shard.reduce_sums(r.sums)
+        r.totals = pgd.close_counts(r.sums, n, m)
+        return r
 
     def step():
+        if sharded:
+            return decompose_span(g)
         g.sort_edges(args.order)
         return g.decompose(micro=True)
 
@@ -370,7 +400,8 @@ def main():
     clk = clocks.stop()
     launches = ctx.kernel_launches - launches0
     window_ms = max_over_ranks(ev0.elapsed_time(ev1))
-    value = world * m * args.steps / (window_ms / 1000.0)
+    units = m if sharded else world * m     # edges decomposed by all ranks together
+    value = units * args.steps / (window_ms / 1000.0)
     ms_per_step = window_ms / args.steps
     log("rank %d: %.1f ms/step, decomposition kernels %.1f ms (k_hub %.1f ms), %.3g edges/s"
         % (rank, ms_per_step, np.mean(kernel_ms), np.mean(hub_ms), value))
@@ -382,7 +413,7 @@ def main():
     # committed ncu summary of the same launch on this workload.
     ev, eu, _ = g.edges(with_order=False)
     anchor_hub = ctx.thresholds()[0]
-    b_alg, units = algorithmic_bytes(ev, eu, n, micro=True, anchor_hub=anchor_hub)
+    b_alg, hub_units = algorithmic_bytes(ev, eu, n, micro=True, anchor_hub=anchor_hub, ids=span_ids)
     hub_s = float(np.mean(hub_ms)) / 1000.0
     peak, peak_src = peaks()
     achieved = b_alg / hub_s / 1e9
@@ -391,7 +422,7 @@ def main():
     l2_bytes = prof.get("l2_bytes")
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-        "traffic": traffic, "kernel": "k_hub", "kernel_ms": 1000.0 * hub_s, "units": units,
+        "traffic": traffic, "kernel": "k_hub", "kernel_ms": 1000.0 * hub_s, "units": hub_units,
         "unit_name": "hub-anchored edges (anchor degree >= %d)" % anchor_hub,
         "algorithmic_bytes": b_alg,
         "dram_frac": (traffic / hub_s / 1e9 / peak) if traffic else None,
@@ -417,7 +448,7 @@ def main():
             ge.preprocess("deg")
             ge.compute_cores()
             ge.sort_edges(args.order)
-            res = ge.decompose(micro=True)
+            res = decompose_span(ge) if sharded else ge.decompose(micro=True)
             lib = pgd.lib()
             st = lib.pgd_get_micro(ge.h, pgd._ptr(h_s1), pgd._ptr(h_d1), pgd._ptr(h_cols))
             assert st == 0
@@ -437,7 +468,7 @@ def main():
         torch.cuda.synchronize()
         barrier()
         e2e_ms = max_over_ranks(e0.elapsed_time(e1)) / args.e2e_steps
-        e2e = {"value": world * m / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
+        e2e = {"value": units / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
                "h2d_bytes_per_step": int(src.nbytes + dst.nbytes),
                "d2h_bytes_per_step": int(m * (pgd.NMICRO * 8 + 12) + (pgd.NTOTALS + pgd.NSUMS) * 8)}
         log("rank %d: e2e %.1f ms/step" % (rank, e2e_ms))
@@ -446,7 +477,7 @@ def main():
     # the reference's benchmark input, an mtx file of the same graph, read by
     # pgd_graph_from_file (one copy of the file's bytes, parsing on the device)
     e2e_file = None
-    if not args.no_e2e and rank == 0:
+    if not args.no_e2e and world == 1:
         import tempfile
 
         tdir = tempfile.mkdtemp(prefix="pgd_bench_")
@@ -529,9 +560,12 @@ def main():
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "strong" if sharded else "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded RMAT generator)",
-            "config": workload_config(args.scale, args.order, n, m), "roofline": roofline,
+            "config": dict(workload_config(args.scale, args.order, n, m),
+                           parallelism=("shard%d" % world if sharded else "replicas%d" % world) if world > 1
+                           else "single GPU"), "roofline": roofline,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
             "totals": {k_: int(v) for k_, v in zip(pgd.TOTAL_NAMES, ref_totals)},
             "e2e_file": e2e_file, "batched": batched, "served": served,

@@ -6,6 +6,7 @@
     python -m benchmarks.suite profile [--scale 18] [--order kcore] [--reps 1]
     python -m benchmarks.suite small [--reps 50]
     python -m benchmarks.suite profile_batch [--graphs 256]
+    python -m benchmarks.suite shard [--scale 20]
 
 batch: 4096 independent graphs, n uniform in [16, 2048]; half G(n, p) with p
 uniform in [0.01, 0.5], half Barabasi-Albert with m uniform in {2..8}; all
@@ -311,6 +312,42 @@ def run_profile(args):
     g.micro()   # the per-edge ids of the output rows (k_micro_ids)
 
 
+def run_shard(args):
+    """The edge-span split of one RMAT graph (pgd_gb300/shard.py) measured
+    span by span on one GPU: each span's sort + decomposition time, their
+    imbalance (max / mean), and the whole graph's time for comparison.  The
+    spans' partial sums must add up to the whole graph's."""
+    from pgd_gb300 import shard
+
+    s, d = pgd.rmat(args.scale, 16, seed=1, **RMAT)
+    ctx = pgd.Context()
+    g = ctx.graph_from_edges(s, d)
+    g.preprocess("deg")
+    g.compute_cores()
+    g.sort_edges(args.order)
+    full = g.decompose(micro=True)
+    full = g.decompose(micro=True)
+    ev, eu, ids = g.edges()
+    deg = np.bincount(ev, minlength=g.n) + np.bincount(eu, minlength=g.n)
+    out = {"mode": "shard", "scale": args.scale, "n": g.n, "m": g.m, "full_kernel_ms": full.kernel_ms, "worlds": {}}
+    for world in (2, 4, 8):
+        for name, cost in (("cost_model", shard.edge_cost(ev, eu, deg, ids, ctx.thresholds()[1])),
+                           ("edge_count", np.ones(len(ids)))):
+            spans = shard.edge_spans(cost, world)
+            times, hub, total = [], [], np.zeros(pgd.NSUMS, np.uint64)
+            for lo, hi in spans:
+                g.sort_edges_sample(ids[lo:hi].astype(np.int64), "natural", s2l=True)
+                r = g.decompose(micro=True)
+                times.append(r.kernel_ms)
+                hub.append(r.hub_ms)
+                total += r.sums
+            assert (total == full.sums).all(), "span sums do not add up"
+            out["worlds"]["%d_%s" % (world, name)] = {
+                "span_kernel_ms": [round(t, 1) for t in times], "max_over_mean": max(times) / np.mean(times),
+                "max_ms": max(times), "speedup_vs_full": full.kernel_ms / max(times)}
+    print(json.dumps(out), flush=True)
+
+
 def run_small(args):
     s, d = pgd.erdos_renyi(250, 0.9, seed=1)
     ctx = pgd.Context()
@@ -410,7 +447,7 @@ def run_large(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("mode", choices=["batch", "serve", "large", "profile", "small", "profile_batch"])
+    ap.add_argument("mode", choices=["batch", "serve", "large", "profile", "small", "profile_batch", "shard"])
     ap.add_argument("--workloads", default="rmat24,rgg24")
     ap.add_argument("--samples", type=int, default=1000)
     ap.add_argument("--heavy", type=int, default=10)
@@ -435,6 +472,8 @@ def main():
         run_small(args)
     elif args.mode == "profile_batch":
         run_profile_batch(args)
+    elif args.mode == "shard":
+        run_shard(args)
     else:
         run_profile(args)
 

@@ -1697,46 +1697,47 @@ struct StageMs {
     float total = 0, tri = 0, hub = 0;
 };
 
-static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int32_t nhubs, int32_t nwide,
-                                int32_t max_degree,
-                                StageMs *ms, const DenseView *dense = nullptr) {
+// The work plan of the positions G.order[0..G.npos): hub-anchored positions
+// grouped by anchor into work items (with their {position, q} records), then
+// dense-graph positions, then light ones (posv).
+struct Plan {
+    int32_t *posv = nullptr;
+    unsigned long long nh = 0, nd = 0;
+    int64_t nlight = 0, nitems = 0;
+    int64_t *items = nullptr;
+    int2 *hrec = nullptr;
+};
+
+static pgd_status build_plan(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, Plan *P, uint64_t **keys_out = nullptr,
+                             int32_t **vals_out = nullptr, uint64_t **keys2_out = nullptr) {
     cudaStream_t s = ctx->stream;
     pgd_status st;
-    const int64_t m = G.npos;   // positions to decompose (E_ordered length)
-    *ms = StageMs();
-    if (m == 0) return PGD_OK;
-    // a sampled order decomposes some edges but reads t(x, q) of any edge
-    const bool sampled = G.npos < G.m;
+    const int64_t m = G.npos;
     uint64_t *keys = nullptr, *keys2 = nullptr;
-    int32_t *posv = nullptr, *vals = nullptr;
+    int32_t *vals = nullptr;
     uint32_t *flag = nullptr, *fpos = nullptr;
-    int64_t *items = nullptr;
-    uint32_t *ghist = nullptr;
-    uint32_t *gbm = nullptr;
-    int2 *hrec = nullptr;
-    int32_t *thigh = nullptr;
-    TmpGuard tg(ctx);
     if ((st = tg.alloc(&keys, m * sizeof(uint64_t)))) return st;
     if ((st = tg.alloc(&keys2, m * sizeof(uint64_t)))) return st;
-    if ((st = tg.alloc(&posv, m * sizeof(int32_t)))) return st;
+    if ((st = tg.alloc(&P->posv, m * sizeof(int32_t)))) return st;
     if ((st = tg.alloc(&vals, m * sizeof(int32_t)))) return st;
-    // [0] hub edges, [1] hub item counter, [2] light counter, [3] dense edges, [4] dense counter
+    // [0] hub edges, [1] hub item counter, [2] light counter, [3] dense edges, [4] dense counter,
+    // [5] triangle-pass item counter
     unsigned long long *ctr = ctx->d_ctr;
     PGD_CUDA(ctx, cudaMemsetAsync(ctr, 0, 8 * sizeof(unsigned long long), s));
-    PGD_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
     PGD_LAUNCH(ctx, k_plan_keys, grid_for(m), kThreads, 0, G, keys, vals, ctr);
     size_t tb = 0;
     void *tmp = nullptr;
-    cub::DeviceRadixSort::SortPairs(nullptr, tb, keys, keys2, vals, posv, m, 0, 64, s);
+    cub::DeviceRadixSort::SortPairs(nullptr, tb, keys, keys2, vals, P->posv, m, 0, 64, s);
     if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
-    cub::DeviceRadixSort::SortPairs(tmp, tb, keys, keys2, vals, posv, m, 0, 64, s);
+    cub::DeviceRadixSort::SortPairs(tmp, tb, keys, keys2, vals, P->posv, m, 0, 64, s);
     pgd_tmp_free(ctx, tmp);
     unsigned long long cnt[4] = {0, 0, 0, 0};
     PGD_CUDA(ctx, cudaMemcpyAsync(cnt, ctr, sizeof(cnt), cudaMemcpyDeviceToHost, s));
     PGD_CUDA(ctx, cudaStreamSynchronize(s));
-    const unsigned long long nh = cnt[0], nd = cnt[3];
-    const int64_t nlight = m - (int64_t)nh - (int64_t)nd;
-    int64_t nitems = 0;
+    P->nh = cnt[0];
+    P->nd = cnt[3];
+    P->nlight = m - (int64_t)P->nh - (int64_t)P->nd;
+    const unsigned long long nh = P->nh;
     if (nh > 0) {
         if ((st = tg.alloc(&flag, (nh + 1) * sizeof(uint32_t)))) return st;
         if ((st = tg.alloc(&fpos, (nh + 1) * sizeof(uint32_t)))) return st;
@@ -1750,44 +1751,102 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
         uint32_t ni = 0;
         PGD_CUDA(ctx, cudaMemcpyAsync(&ni, fpos + nh, sizeof(ni), cudaMemcpyDeviceToHost, s));
         PGD_CUDA(ctx, cudaStreamSynchronize(s));
-        nitems = ni;
-        if ((st = tg.alloc(&items, (nitems + 1) * sizeof(int64_t)))) return st;
-        PGD_LAUNCH(ctx, k_item_fill, grid_for(nh), kThreads, 0, flag, fpos, (int64_t)nh, items);
-        if ((st = tg.alloc(&hrec, (nh + 1) * sizeof(int2)))) return st;
-        PGD_LAUNCH(ctx, k_hub_recs, grid_for(nh), kThreads, 0, G, posv, (int64_t)nh, hrec);
+        P->nitems = ni;
+        if ((st = tg.alloc(&P->items, (P->nitems + 1) * sizeof(int64_t)))) return st;
+        PGD_LAUNCH(ctx, k_item_fill, grid_for(nh), kThreads, 0, flag, fpos, (int64_t)nh, P->items);
+        if ((st = tg.alloc(&P->hrec, (nh + 1) * sizeof(int2)))) return st;
+        PGD_LAUNCH(ctx, k_hub_recs, grid_for(nh), kThreads, 0, G, P->posv, (int64_t)nh, P->hrec);
     }
+    if (keys_out) *keys_out = keys;
+    if (vals_out) *vals_out = vals;
+    if (keys2_out) *keys2_out = keys2;
+    return PGD_OK;
+}
+
+// t of the edges of a plan, written to both slots of each: hub-anchored
+// edges grouped by anchor (k_tslot_hub), the rest one warp each.
+static pgd_status triangle_pass(pgd_ctx *ctx, const DevGraph &G, int4 *slot, const Plan &P, const HubArgs &H,
+                                uint32_t *gbm) {
     const int nsm = ctx->num_sms;
-    // triangle counts of every edge first: k_hub and k_light read t(x, q) of
-    // other edges.  Hub-anchored edges grouped by anchor, the rest one warp each
-    // (dense-graph edges need none).
-    HubArgs H;
-    const size_t smem = hub_layout(G.n, nhubs, nwide, max_degree, &H);
-    PGD_CUDA(ctx, cudaEventRecord(ctx->evt0, s));
-    if (sampled) PGD_LAUNCH(ctx, k_tslot, grid_for(32 * G.m), kThreads, 0, G, slot, nullptr, 0);
-    if (nitems > 0) {
-        if ((int64_t)H.split < G.n) {
-            if ((st = tg.alloc(&gbm, (size_t)nsm * H.nwords * 4))) return st;
-            PGD_CUDA(ctx, cudaMemsetAsync(gbm, 0, (size_t)nsm * H.nwords * 4, s));
-        }
+    if (P.nitems > 0) {
         HubArgs T = H;
         T.G = G;
-        T.hrec = hrec;
-        T.items = items;
-        T.nitems = nitems;
+        T.hrec = P.hrec;
+        T.items = P.items;
+        T.nitems = P.nitems;
         T.gbitmap = gbm;
-        T.next = ctr + 5;
+        T.next = ctx->d_ctr + 5;
         T.slot_out = slot;
         // the whole dynamic shared memory holds bitmap ranks (no histogram here)
         const int64_t tw = std::min<int64_t>(H.nwords, kMaxTslotSmem / 4);
         T.split = (int32_t)std::min<int64_t>(tw * 32, 0x7fffffe0);
-        if (!sampled) {
-            PGD_CUDA(ctx, cudaFuncSetAttribute(k_tslot_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(tw * 4)));
-            PGD_LAUNCH(ctx, k_tslot_hub, nsm, kHubWarps * 32, (size_t)(tw * 4), T);
-        }
+        PGD_CUDA(ctx, cudaFuncSetAttribute(k_tslot_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(tw * 4)));
+        PGD_LAUNCH(ctx, k_tslot_hub, nsm, kHubWarps * 32, (size_t)(tw * 4), T);
     }
-    if (nlight > 0 && !sampled)
-        PGD_LAUNCH(ctx, k_tslot, grid_for(32 * nlight), kThreads, 0, G, slot, posv + nh + nd, nlight);
-    PGD_CUDA(ctx, cudaEventRecord(ctx->evt1, s));
+    if (P.nlight > 0)
+        PGD_LAUNCH(ctx, k_tslot, grid_for(32 * P.nlight), kThreads, 0, G, slot, P.posv + P.nh + P.nd, P.nlight);
+    return PGD_OK;
+}
+
+__global__ void k_iota(int32_t *a, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = (int32_t)i;
+}
+
+static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int32_t nhubs, int32_t nwide,
+                                int32_t max_degree,
+                                StageMs *ms, const DenseView *dense = nullptr) {
+    cudaStream_t s = ctx->stream;
+    pgd_status st;
+    const int64_t m = G.npos;   // positions to decompose (E_ordered length)
+    *ms = StageMs();
+    if (m == 0) return PGD_OK;
+    // a sampled order decomposes some edges but reads t(x, q) of any edge
+    const bool sampled = G.npos < G.m;
+    uint32_t *ghist = nullptr;
+    uint32_t *gbm = nullptr;
+    int32_t *thigh = nullptr;
+    TmpGuard tg(ctx);
+    const int nsm = ctx->num_sms;
+    HubArgs H;
+    const size_t smem = hub_layout(G.n, nhubs, nwide, max_degree, &H);
+    if ((int64_t)H.split < G.n) {
+        if ((st = tg.alloc(&gbm, (size_t)nsm * H.nwords * 4))) return st;
+        PGD_CUDA(ctx, cudaMemsetAsync(gbm, 0, (size_t)nsm * H.nwords * 4, s));
+    }
+    PGD_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
+    // triangle counts of every edge first: k_hub and k_light read t(x, q) of
+    // other edges.  A sampled order still needs t of all edges: the same
+    // grouped pass runs over a plan of every edge (positions = edge ids).
+    if (sampled) {
+        int32_t *iota = nullptr;
+        if ((st = tg.alloc(&iota, (size_t)G.m * sizeof(int32_t)))) return st;
+        PGD_LAUNCH(ctx, k_iota, grid_for(G.m), kThreads, 0, iota, G.m);
+        DevGraph GA = G;
+        GA.order = iota;
+        GA.npos = G.m;
+        GA.micro = nullptr;
+        Plan PA;
+        if ((st = build_plan(ctx, GA, tg, &PA))) return st;
+        PGD_CUDA(ctx, cudaEventRecord(ctx->evt0, s));
+        if ((st = triangle_pass(ctx, GA, slot, PA, H, gbm))) return st;
+        PGD_CUDA(ctx, cudaEventRecord(ctx->evt1, s));
+    }
+    Plan P;
+    uint64_t *keys = nullptr, *keys2 = nullptr;
+    int32_t *vals = nullptr;
+    if ((st = build_plan(ctx, G, tg, &P, &keys, &vals, &keys2))) return st;
+    int32_t *posv = P.posv;
+    const unsigned long long nh = P.nh, nd = P.nd;
+    const int64_t nlight = P.nlight, nitems = P.nitems;
+    int64_t *items = P.items;
+    int2 *hrec = P.hrec;
+    unsigned long long *ctr = ctx->d_ctr;
+    if (!sampled) {
+        PGD_CUDA(ctx, cudaEventRecord(ctx->evt0, s));
+        if ((st = triangle_pass(ctx, G, slot, P, H, gbm))) return st;
+        PGD_CUDA(ctx, cudaEventRecord(ctx->evt1, s));
+    }
     if (nitems > 0) {
         if (!H.smem_hist) {
             if ((st = tg.alloc(&ghist, (size_t)nsm * H.hstride * 4))) return st;

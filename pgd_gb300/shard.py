@@ -2,8 +2,12 @@
 
 Edges are independent given the CSR, so every rank holds the whole graph and
 decomposes a contiguous span of the ordered edge list (E_ordered).  The spans
-are weighted by an estimate of each edge's work, the degree of its cheaper
-endpoint.  Each rank orders and decomposes its span with the sampled edge
+are weighted by an estimate of each edge's work in the decomposition kernels:
+the scan of the non-anchor endpoint q's list plus the lists of its
+low-degree neighbours, which are scanned per edge (see edge_cost).  Every
+rank also computes the triangle count of every edge (the c4 identity reads
+t of edges outside the span) and the graph's per-vertex structures: that
+O(m) part is repeated on each rank and bounds strong scaling.  Each rank orders and decomposes its span with the sampled edge
 order (`Graph.sort_edges_sample`, the reference's sort_edges with E_s,
 graphlet_core.cpp:836-851).  The only exchange is a sum of the 15 uint64
 partial sums, which wraps mod 2^64 exactly like the device sums.  The 17
@@ -36,12 +40,22 @@ def edge_spans(cost, world):
     return [(bounds[i], bounds[i + 1]) for i in range(world)]
 
 
-def edge_cost(ev, eu, deg, order):
-    """Work estimate of each ordered edge: the degree of its cheaper endpoint
-    plus one (the list the decomposition scans)."""
-    ev = np.asarray(ev)[order]
-    eu = np.asarray(eu)[order]
-    return np.minimum(deg[ev], deg[eu]).astype(np.float64) + 1.0
+def edge_cost(ev, eu, deg, order, cache_hub=40):
+    """Work estimate of each ordered edge (p, q), p the endpoint of higher
+    (degree, id): deg(q) slot records, plus the lists of q's neighbours of
+    degree below cache_hub (their W(w, p) is counted per edge, the higher
+    ones come from the anchor's histogram), plus one."""
+    ev = np.asarray(ev, np.int64)
+    eu = np.asarray(eu, np.int64)
+    deg = np.asarray(deg, np.int64)
+    n = len(deg)
+    dv, du = deg[ev], deg[eu]
+    small = np.bincount(ev, weights=np.where(du < cache_hub, du, 0), minlength=n) + \
+        np.bincount(eu, weights=np.where(dv < cache_hub, dv, 0), minlength=n)
+    a, b = ev[order], eu[order]
+    da, db = deg[a], deg[b]
+    q = np.where((da > db) | ((da == db) & (a > b)), b, a)
+    return deg[q].astype(np.float64) + small[q] + 1.0
 
 
 def reduce_sums(sums, group=None):
@@ -52,8 +66,10 @@ def reduce_sums(sums, group=None):
 
     t = torch.from_numpy(np.ascontiguousarray(sums, dtype=np.uint64).view(np.int64).copy())
     if dist.is_available() and dist.is_initialized():
+        if dist.get_backend(group) == "nccl":   # NCCL reduces device tensors
+            t = t.cuda()
         dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
-    return t.numpy().view(np.uint64).copy()
+    return t.cpu().numpy().view(np.uint64).copy()
 
 
 def sharded_totals(span_sums, n, m, close_counts, group=None):

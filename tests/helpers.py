@@ -17,10 +17,17 @@ def load_npz(name):
     return np.load(os.path.join(GOLDEN, name), allow_pickle=False)
 
 
-def rows_digest(src, dst, cols):
-    rows = np.concatenate([np.asarray(src, np.uint64)[:, None], np.asarray(dst, np.uint64)[:, None],
-                           np.asarray(cols, np.uint64)], axis=1)
-    return hashlib.sha256(np.ascontiguousarray(rows, "<u8").tobytes()).hexdigest()
+def rows_digest(src, dst, cols, chunk=1 << 20):
+    """SHA-256 of the rows (src, dst, 8 columns) as little-endian uint64,
+    hashed a chunk of rows at a time (the same digest as one pass over the
+    whole table, without building it)."""
+    h = hashlib.sha256()
+    for i in range(0, len(cols), chunk):
+        rows = np.concatenate([np.asarray(src[i:i + chunk], np.uint64)[:, None],
+                               np.asarray(dst[i:i + chunk], np.uint64)[:, None],
+                               np.asarray(cols[i:i + chunk], np.uint64)], axis=1)
+        h.update(np.ascontiguousarray(rows, "<u8").tobytes())
+    return h.hexdigest()
 
 
 def mtx_pairs(u, v):
