@@ -275,10 +275,10 @@ pgd_status pgd_server_destroy(pgd_server *sv);
 
 /* ---- thresholds and autotuning (no reference counterpart) --------------
  * Three thresholds steer how the decomposition kernels split work; counts
- * never depend on them.  anchor_hub (2..256, default 128): anchors of degree
+ * never depend on them.  anchor_hub (2..256, default 64): anchors of degree
  * >= it are processed one CTA per anchor with N(p) as a bitmap, below it one
  * warp per edge with N(p) staged and searched.  cache_hub (>= 2, default
- * 40): W(w,p) comes from the anchor's histogram for neighbours of degree >=
+ * 32): W(w,p) comes from the anchor's histogram for neighbours of degree >=
  * it (16-bit counters from degree 256, 8-bit below), below it N(w) is
  * scanned per edge.  dense_max (0..2048, default 2048): in a batch,
  * graphs of at most this many vertices are decomposed with whole adjacency

@@ -24,8 +24,8 @@ struct pgd_ctx {
     cudaEvent_t evt0 = nullptr, evt1 = nullptr, evh0 = nullptr, evh1 = nullptr;
     unsigned long long launches = 0;        // kernels of this library launched
     // decomposition thresholds (results never depend on them; pgd_autotune sets them)
-    int anchor_hub = 128;    // anchors of degree >= this take the bitmap (block) path
-    int cache_hub = 40;      // W(w,p) taken from the per-anchor histogram for neighbours of degree >= this
+    int anchor_hub = 64;     // anchors of degree >= this take the bitmap (block) path
+    int cache_hub = 32;      // W(w,p) taken from the per-anchor histogram for neighbours of degree >= this
     int dense_max = 2048;    // batched graphs with at most this many vertices use row bitsets
 };
 
