@@ -5,7 +5,8 @@ order: about 6.7 h on 8 cores), so the fixture comes from the oracle
 (oracle/pgd_oracle.c), whose parity with the reference is pinned by
 tests/test_oracle.py on every graph the reference finishes, including the
 reference's RMAT-18 totals.  One run of the oracle's full per-edge loop per
-graph, all host threads (about half an hour for RMAT-20 on 8 cores).
+graph, all host threads (about 20 minutes for RMAT-20 and 6 for the 3-D RGG
+with n = 2^24 on 8 cores; the latter needs about 45 GB of host memory).
 
 Writes, per graph, tests/golden/<name>.json:
   generator arguments and the SHA-256 of the raw input pairs,

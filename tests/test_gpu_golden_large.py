@@ -1,6 +1,7 @@
 """Full-size pins: the RMAT scale-20 graph in k-core order (the benchmark's
-workload) and the 3-D random geometric graph with n = 2^20, decomposed on the
-GPU and compared bit for bit with the oracle's full runs (every per-edge row,
+workload) and the 3-D random geometric graphs with n = 2^20 and n = 2^24
+(200 M edges), decomposed on the GPU and compared bit for bit with the
+oracle's full runs (every per-edge row,
 in E_ordered order, through its SHA-256; the 17 totals; the 15 raw sums).
 The fixtures come from tests/golden/make_large_golden.py."""
 import json
@@ -28,7 +29,7 @@ def pairs_of(case):
     return pgd.rgg3d(n, r, seed=case["seed"])
 
 
-@pytest.mark.parametrize("name", ["rmat20_kcore", "rgg20_kcore"])
+@pytest.mark.parametrize("name", ["rmat20_kcore", "rgg20_kcore", "rgg24_kcore"])
 def test_full_graph_bit_exact(ctx, name):
     gold = load(name)
     src, dst = pairs_of(gold["case"])
