@@ -61,7 +61,7 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def workload_config(scale, order, n=None, m=None):
+def workload_config(scale, order, n=None, m=None, world=1, mode="shard"):
     cfg = {
         "workload": "rmat%d_%s_global+micro" % (scale, order),
         "graph": "RMAT scale %d, edge factor 16, (a,b,c,d)=(0.57,0.19,0.19,0.05), seed 1, symmetrised, "
@@ -74,6 +74,8 @@ def workload_config(scale, order, n=None, m=None):
     if n is not None:
         cfg["n"] = int(n)
         cfg["m"] = int(m)
+    if world > 1:
+        cfg["parallelism"] = "%s%d" % ("shard" if mode == "shard" else "replicas", world)
     return cfg
 
 
@@ -259,7 +261,8 @@ def run_reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / max(1, args.steps),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-        "data": "synthetic (seeded RMAT generator)", "config": workload_config(args.scale, args.order, n, m),
+        "data": "synthetic (seeded RMAT generator)",
+        "config": workload_config(args.scale, args.order, n, m, int(os.environ.get("WORLD_SIZE", "1")), args.mode),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -563,9 +566,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "strong" if sharded else "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded RMAT generator)",
-            "config": dict(workload_config(args.scale, args.order, n, m),
-                           parallelism=("shard%d" % world if sharded else "replicas%d" % world) if world > 1
-                           else "single GPU"), "roofline": roofline,
+            "config": workload_config(args.scale, args.order, n, m, world, args.mode), "roofline": roofline,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
             "totals": {k_: int(v) for k_, v in zip(pgd.TOTAL_NAMES, ref_totals)},
             "e2e_file": e2e_file, "batched": batched, "served": served,

@@ -883,8 +883,10 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                         for (; i < ln; i += 32) k4 += in_t(Rw, A, bm, Nq, dq, LR + i, __ldg(L + i), th) ? 1 : 0;
                     }
                 }
-                // short lists: flattened over the warp
+                // short lists: flattened over the warp (a short row counts its
+                // 64-bit words)
                 if (len >= 64) len = 0;
+                if (kind == 2) len >>= 1;
                 const int incl = pgd_warp_incl_scan(len);
                 const int total = __shfl_sync(0xffffffffu, incl, 31);
                 const int excl = incl - len;
@@ -900,16 +902,19 @@ __global__ void __launch_bounds__(kHubWarps * 32, 1) k_hub(HubArgs A) {
                     const int okB = __shfl_sync(0xffffffffu, kind, ownB);
                     const int idxB = itB - __shfl_sync(0xffffffffu, excl, ownB);
                     const bool vA = itA < total, vB = itB < total;
-                    const int32_t xA = vA ? __ldg(olA + idxA) : 0, xB = vB ? __ldg(olB + idxB) : 0;
+                    const unsigned long long *t64 = (const unsigned long long *)Rw;
+                    unsigned long long xA = 0, xB = 0;
+                    if (vA) xA = okA == 2 ? __ldg((const unsigned long long *)olA + idxA) : (uint32_t)__ldg(olA + idxA);
+                    if (vB) xB = okB == 2 ? __ldg((const unsigned long long *)olB + idxB) : (uint32_t)__ldg(olB + idxB);
                     if (vA) {
-                        if (okA == 0) sumW += bm.test(xA);
-                        else if (okA == 2) k4 += __popc((uint32_t)xA & Rw[idxA]);
-                        else k4 += in_t(Rw, A, bm, Nq, dq, orA + idxA, xA, th) ? 1 : 0;
+                        if (okA == 0) sumW += bm.test((int32_t)xA);
+                        else if (okA == 2) k4 += __popcll(xA & t64[idxA]);
+                        else k4 += in_t(Rw, A, bm, Nq, dq, orA + idxA, (int32_t)xA, th) ? 1 : 0;
                     }
                     if (vB) {
-                        if (okB == 0) sumW += bm.test(xB);
-                        else if (okB == 2) k4 += __popc((uint32_t)xB & Rw[idxB]);
-                        else k4 += in_t(Rw, A, bm, Nq, dq, orB + idxB, xB, th) ? 1 : 0;
+                        if (okB == 0) sumW += bm.test((int32_t)xB);
+                        else if (okB == 2) k4 += __popcll(xB & t64[idxB]);
+                        else k4 += in_t(Rw, A, bm, Nq, dq, orB + idxB, (int32_t)xB, th) ? 1 : 0;
                     }
                 }
             }
