@@ -206,10 +206,11 @@ __global__ void k_edge_arrays(const int32_t *row, const int32_t *adj, const int3
 // ---------------------------------------------------------------------------
 // k-core peeling.  core[v] = -1 while v is alive.
 
-__global__ void k_core_init(const int32_t *deg, int64_t n, int32_t *cur, int32_t *core) {
+__global__ void k_core_init(const int32_t *deg, int64_t n, int32_t *cur, int32_t *core, int32_t *alive) {
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
         cur[v] = deg[v];
         core[v] = -1;
+        alive[v] = (int32_t)v;
     }
 }
 
@@ -560,35 +561,46 @@ pgd_status pgd_dev_preprocess(pgd_graph *g, int neigh_kind, int s2l) {
 // (a level scan or a peel round, chosen from the state) and a one-thread
 // control kernel that applies the transition; a block of kCoreSteps steps is
 // captured once as a CUDA graph and replayed until the control kernel
-// reports that every vertex has a core number.
+// reports that every vertex has a core number.  A level scan reads only the
+// vertices still alive at the previous scan (a compacted list, rewritten by
+// each scan), so the scans shrink as the peeling goes inward.
 namespace {
 
 struct CoreState {
     int level, mode, sel, done, failed, min_rest;
     unsigned int cnt[2];          // frontier sizes of buffers 0 and 1
     long long removed, steps, max_steps;
+    int asel;                     // alive list read by the next scan
+    unsigned int acnt[2];         // alive list sizes
 };
 
 constexpr int kCoreSteps = 64;
 enum { kCoreScan = 0, kCorePeel = 1 };
 
 __global__ void k_core_work(const int64_t *off, const int32_t *adj, int32_t *cur, int32_t *core, int64_t n,
-                            int32_t *f0, int32_t *f1, CoreState *st) {
+                            int32_t *f0, int32_t *f1, int32_t *a0, int32_t *a1, CoreState *st) {
     if (st->done) return;
     const int mode = st->mode, level = st->level, sel = st->sel;
     int32_t *fin = sel ? f1 : f0, *fout = sel ? f0 : f1;
     if (mode == kCoreScan) {
-        // every alive vertex with cur <= level leaves now; the smallest cur
-        // among the rest lets the control kernel skip empty levels
+        // every alive vertex with cur <= level leaves now; the others are
+        // kept in the next alive list, and the smallest cur among them lets
+        // the control kernel skip empty levels
+        const int asel = st->asel;
+        const int32_t *ain = asel ? a1 : a0;
+        int32_t *aout = asel ? a0 : a1;
+        const unsigned int na = st->acnt[asel];
         int local_min = INT_MAX;
-        for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < na; i += (int64_t)gridDim.x * blockDim.x) {
+            const int32_t v = ain[i];
             if (core[v] != -1) continue;
             const int c = cur[v];
             if (c <= level) {
                 core[v] = level;
-                fin[atomicAdd(&st->cnt[sel], 1u)] = (int32_t)v;
+                fin[atomicAdd(&st->cnt[sel], 1u)] = v;
             } else {
                 local_min = min(local_min, c);
+                aout[atomicAdd(&st->acnt[asel ^ 1], 1u)] = v;
             }
         }
         for (int o = 16; o > 0; o >>= 1) local_min = min(local_min, __shfl_xor_sync(0xffffffffu, local_min, o));
@@ -619,6 +631,9 @@ __global__ void k_core_ctrl(CoreState *st, int64_t n) {
     if (st->done) return;
     const int sel = st->sel;
     if (st->mode == kCoreScan) {
+        // the scan's survivors are the next alive list
+        st->asel ^= 1;
+        st->acnt[st->asel ^ 1] = 0;
         const unsigned int f = st->cnt[sel];
         if (f == 0) {
             // nobody at this level: jump to the smallest remaining count
@@ -661,24 +676,31 @@ pgd_status pgd_dev_cores(pgd_graph *g) {
         if ((st = pgd_graph_alloc(g, (void **)&g->core, (n + 1) * sizeof(int32_t)))) return st;
     }
     if (n == 0) { g->has_cores = true; g->max_core = 0; return PGD_OK; }
-    int32_t *cur = nullptr, *fa = nullptr, *fb = nullptr;
+    int32_t *cur = nullptr, *fa = nullptr, *fb = nullptr, *aa = nullptr, *ab = nullptr;
     CoreState *d_st = nullptr;
     if ((st = pgd_tmp_alloc(ctx, (void **)&cur, n * sizeof(int32_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&fa, n * sizeof(int32_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&fb, n * sizeof(int32_t)))) return st;
+    if ((st = pgd_tmp_alloc(ctx, (void **)&aa, n * sizeof(int32_t)))) return st;
+    if ((st = pgd_tmp_alloc(ctx, (void **)&ab, n * sizeof(int32_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&d_st, sizeof(CoreState)))) return st;
     auto release = [&]() {
         pgd_tmp_free(ctx, cur);
         pgd_tmp_free(ctx, fa);
         pgd_tmp_free(ctx, fb);
+        pgd_tmp_free(ctx, aa);
+        pgd_tmp_free(ctx, ab);
         pgd_tmp_free(ctx, d_st);
     };
-    PGD_LAUNCH(ctx, k_core_init, grid_for(n), kThreads, 0, g->deg, n, cur, g->core);
+    PGD_LAUNCH(ctx, k_core_init, grid_for(n), kThreads, 0, g->deg, n, cur, g->core, aa);
     // every step removes a vertex or raises the level (at most max_degree + 1
     // levels), so 2 (n + max_degree) + 4 steps always suffice
     CoreState h{};
     h.min_rest = INT_MAX;
     h.max_steps = 2 * (n + (long long)g->max_degree) + 4;
+    h.asel = 0;
+    h.acnt[0] = (unsigned int)n;   // every vertex alive at the first scan
+    h.acnt[1] = 0;
     PGD_CUDA(ctx, cudaMemcpyAsync(d_st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
     const int work_grid = grid_for(32 * (int64_t)ctx->num_sms * 64);
     // capture kCoreSteps steps once, replay until done
@@ -687,7 +709,7 @@ pgd_status pgd_dev_cores(pgd_graph *g) {
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         for (int i = 0; i < kCoreSteps; i++) {
-            k_core_work<<<work_grid, kThreads, 0, s>>>(g->off, g->adj, cur, g->core, n, fa, fb, d_st);
+            k_core_work<<<work_grid, kThreads, 0, s>>>(g->off, g->adj, cur, g->core, n, fa, fb, aa, ab, d_st);
             k_core_ctrl<<<1, 1, 0, s>>>(d_st, n);
         }
         e = cudaStreamEndCapture(s, &graph);
