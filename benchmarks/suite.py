@@ -135,6 +135,7 @@ def run_batch(args, emit=True):
     # autotune on a stratified sample (every 16th graph)
     sample = [ctx.graph_from_edges(s, d) for s, d in graphs[:: max(1, len(graphs) // 256)]]
     a, c, dm, ms = ctx.autotune(sample, reps=1)
+    tmd = ctx.tensor_min_degree()
     for g in sample:
         g.destroy()
     log("autotuned thresholds: anchor_hub=%d cache_hub=%d dense_max=%d" % (a, c, dm))
@@ -178,7 +179,7 @@ def run_batch(args, emit=True):
         "speedup_vs_single_graph_api": (len(graphs) / best) / max(plain["single_graph_api_default"],
                                                                   plain["single_graph_api_tuned"]),
         "speedup_vs_batch_of_one": (len(graphs) / best) / plain["batch_of_one"],
-        "thresholds": {"anchor_hub": a, "cache_hub": c, "dense_max": dm},
+        "thresholds": {"anchor_hub": a, "cache_hub": c, "dense_max": dm, "tensor_min_degree": tmd},
         "workload": "%d graphs, n~U[16,2048], half G(n,p) p~U[0.01,0.5], half BA m~U{2..8}, seed %d"
                     % (len(graphs), args.seed),
     }
@@ -292,9 +293,14 @@ def run_profile_batch(args):
     graphs, _ = batch_graphs(args.graphs, args.seed)
     ctx = pgd.Context()
     ctx.set_thresholds(64, 128, 2048)
-    res = ctx.decompose_pairs_batch(graphs)
+    if args.tensor_min_degree >= 0:
+        ctx.set_tensor_min_degree(args.tensor_min_degree)
+    res = None
+    for _ in range(max(1, args.reps)):
+        res = ctx.decompose_pairs_batch(graphs)
     print(json.dumps({"mode": "profile_batch", "graphs": len(graphs), "pairs": sum(len(s) for s, _ in graphs),
-                      "kernel_ms": float(res[0].kernel_ms)}), flush=True)
+                      "tensor_min_degree": ctx.tensor_min_degree(), "kernel_ms": float(res[0].kernel_ms)}),
+          flush=True)
 
 
 def run_profile(args):
@@ -461,6 +467,7 @@ def main():
     ap.add_argument("--reps", type=int, default=3)  # batch: timed repetitions; profile: decompositions
     ap.add_argument("--plain-sample", type=int, default=256)
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--tensor-min-degree", type=int, default=-1, help="profile_batch: -1 keeps the default")
     args = ap.parse_args()
     if args.mode == "batch":
         run_batch(args)

@@ -285,12 +285,20 @@ pgd_status pgd_server_destroy(pgd_server *sv);
  * rows as bitsets (one 2048-bit row per warp), larger ones with sorted
  * lists; those of average degree >= n/16 also get a 16-bit common-neighbour
  * matrix (about 2·n² bytes of device memory while the batch runs).
+ * A fourth, tensor_min_degree (0 or 2..1152, default 128): in those
+ * common-neighbour graphs, the edges (p, q) whose lower-degree endpoint q has
+ * degree in [tensor_min_degree, 1152] get their 4-clique count from a
+ * product of q's ego network on the tensor cores (e4m3 0/1 operands, fp32
+ * sums, exact); 0 keeps every edge on the integer path.
  * pgd_autotune decomposes the given graphs `reps` times per
- * candidate -- first dense_max in {0, 256, 1024, 2048}, then 16
- * (anchor_hub, cache_hub) pairs -- checks that every candidate gives
- * identical counts, keeps the fastest on the context and reports it. */
+ * candidate -- first dense_max in {0, 256, 1024, 2048}, then
+ * tensor_min_degree in {0, 64, 128, 256}, then 16 (anchor_hub, cache_hub)
+ * pairs -- checks that every candidate gives identical counts, keeps the
+ * fastest on the context and reports it. */
 pgd_status pgd_set_thresholds(pgd_ctx *ctx, int anchor_hub, int cache_hub, int dense_max);
 pgd_status pgd_get_thresholds(const pgd_ctx *ctx, int *anchor_hub, int *cache_hub, int *dense_max);
+pgd_status pgd_set_tensor_min_degree(pgd_ctx *ctx, int tensor_min_degree);
+pgd_status pgd_get_tensor_min_degree(const pgd_ctx *ctx, int *tensor_min_degree);
 pgd_status pgd_autotune(pgd_ctx *ctx, pgd_graph *const *graphs, int k, int reps, int *anchor_hub, int *cache_hub,
                         int *dense_max, float *best_ms);
 

@@ -48,7 +48,7 @@ EXPORTS = [
     "pgd_gen_rgg3d", "pgd_decompose_csr_noalloc", "pgd_noalloc_scratch_bytes", "pgd_set_thresholds",
     "pgd_get_thresholds", "pgd_autotune", "pgd_decompose_pairs_batch", "pgd_server_create", "pgd_server_submit",
     "pgd_server_poll", "pgd_server_wait", "pgd_server_stats", "pgd_server_destroy", "pgd_sort_edges_sample",
-    "pgd_graph_order_length",
+    "pgd_graph_order_length", "pgd_set_tensor_min_degree", "pgd_get_tensor_min_degree",
 ]
 
 
@@ -147,6 +147,8 @@ def lib():
                                                          ctypes.c_size_t]),
             "pgd_noalloc_scratch_bytes": (ctypes.c_uint64, []),
             "pgd_set_thresholds": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+            "pgd_set_tensor_min_degree": (ctypes.c_int, [_P, ctypes.c_int]),
+            "pgd_get_tensor_min_degree": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
             "pgd_decompose_pairs_batch": (ctypes.c_int, [_P, ctypes.c_int, _I64, _I32, _I32, _P,
                                                          ctypes.POINTER(pgd_counts)]),
             "pgd_server_create": (ctypes.c_int, [ctypes.POINTER(pgd_server_opts), _PP]),
@@ -262,6 +264,15 @@ class Context:
         self._check(lib().pgd_get_thresholds(self.h, ctypes.byref(a), ctypes.byref(c), ctypes.byref(d)),
                     "pgd_get_thresholds")
         return a.value, c.value, d.value
+
+    def set_tensor_min_degree(self, d):
+        """Dense batch graphs: runs with q of degree in [d, 1152] count k4 on the tensor cores (0: never)."""
+        self._check(lib().pgd_set_tensor_min_degree(self.h, d), "pgd_set_tensor_min_degree")
+
+    def tensor_min_degree(self):
+        d = ctypes.c_int()
+        self._check(lib().pgd_get_tensor_min_degree(self.h, ctypes.byref(d)), "pgd_get_tensor_min_degree")
+        return d.value
 
     def autotune(self, graphs, reps=1):
         """Pick the fastest thresholds for these graphs; returns (anchor_hub, cache_hub, dense_max, ms)."""

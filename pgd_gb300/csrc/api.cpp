@@ -445,6 +445,20 @@ extern "C" pgd_status pgd_get_thresholds(const pgd_ctx *ctx, int *anchor_hub, in
     return PGD_OK;
 }
 
+extern "C" pgd_status pgd_set_tensor_min_degree(pgd_ctx *ctx, int tensor_min_degree) {
+    if (!ctx) return PGD_EINVAL;
+    if (tensor_min_degree != 0 && (tensor_min_degree < 2 || tensor_min_degree > 1152))
+        return pgd_fail(ctx, PGD_EINVAL, "tensor_min_degree out of range (0, or 2..1152)");
+    ctx->tc_min_deg = tensor_min_degree;
+    return PGD_OK;
+}
+
+extern "C" pgd_status pgd_get_tensor_min_degree(const pgd_ctx *ctx, int *tensor_min_degree) {
+    if (!ctx) return PGD_EINVAL;
+    if (tensor_min_degree) *tensor_min_degree = ctx->tc_min_deg;
+    return PGD_OK;
+}
+
 extern "C" pgd_status pgd_autotune(pgd_ctx *ctx, pgd_graph *const *graphs, int k, int reps, int *anchor_hub,
                                    int *cache_hub, int *dense_max, float *best_ms) {
     if (!ctx || k <= 0 || !graphs) return pgd_fail(ctx, PGD_EINVAL, "bad arguments");
@@ -466,7 +480,7 @@ extern "C" pgd_status pgd_autotune(pgd_ctx *ctx, pgd_graph *const *graphs, int k
         *ms = total / reps;
         return PGD_OK;
     };
-    // 1. the bitset/list crossover for small graphs, 2. the two hub thresholds
+    // 1. the bitset/list crossover for small graphs
     float best = -1, ms = 0;
     int bd = ctx->dense_max;
     for (int d : {0, 256, 1024, 2048}) {
@@ -476,6 +490,17 @@ extern "C" pgd_status pgd_autotune(pgd_ctx *ctx, pgd_graph *const *graphs, int k
         if (best < 0 || ms < best) { best = ms; bd = d; }
     }
     ctx->dense_max = bd;
+    // 2. which runs of the dense graphs go to the tensor cores
+    best = -1;
+    int bt = ctx->tc_min_deg;
+    for (int t : {0, 64, 128, 256}) {
+        ctx->tc_min_deg = t;
+        pgd_status st = trial(&ms);
+        if (st) return st;
+        if (best < 0 || ms < best) { best = ms; bt = t; }
+    }
+    ctx->tc_min_deg = bt;
+    // 3. the two hub thresholds
     best = -1;
     int ba = ctx->anchor_hub, bc = ctx->cache_hub;
     for (int a : {32, 64, 128, 256}) {

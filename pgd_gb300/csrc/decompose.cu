@@ -49,6 +49,7 @@
 
 #include "pgd_internal.h"
 #include "pgd_kernels.cuh"
+#include "tc_ptx.cuh"
 
 namespace {
 
@@ -1361,6 +1362,7 @@ struct DenseCnArgs {
     const uint16_t *cn;       // CN matrices of the graphs that have one
     const int64_t *cbase;     // per graph: first entry of its CN matrix
     const int32_t *dpos;      // E_ordered positions of those graphs' edges, grouped by q
+    const uint32_t *k4pre;    // per position of dpos: k4 from k_dense_tc, 0xffffffff where not taken (or null)
     int64_t ndense;
     unsigned long long *next;
 };
@@ -1368,6 +1370,9 @@ struct DenseCnArgs {
 // Up to kDenseGroup edges (p_j, q) with the same q, as in k_dense; per row
 // word L of A_q the warp reads 64 entries of CN[q] and of each CN[p_j] (two
 // per lane) for the two sums, and the rows of the word's members of T_j.
+// kPre: only the groups whose k4 k_dense_tc counted (no scan of T's rows);
+// otherwise only the others.
+template <bool kPre>
 __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
     __shared__ unsigned long long s_red[8][PGD_NSUMS];
     const DevGraph &G = A.G;
@@ -1394,6 +1399,12 @@ __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
             const int64_t stride = (int64_t)W * 64;
             const uint64_t *rows = A.bits + A.wbase[g];
             const uint16_t *cnb = A.cn + A.cbase[g];
+            // k4 of this group counted on the tensor cores or not (all edges of a
+            // group share q, so all or none are): the other instance takes it
+            if ((A.k4pre && A.k4pre[i0] != 0xffffffffu) != kPre) {
+                i0 = i1;
+                continue;
+            }
             const int64_t q = qg - vb;
             const uint16_t *cq = cnb + q * stride;
             const uint64_t Aq = lane < W ? __ldg(rows + q * W + lane) : 0ull;
@@ -1449,7 +1460,7 @@ __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
                 // rows of this word's members of the T_j (k4), one half at a
                 // time, two rows in flight, each row tested against every T_j
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
+                for (int h = 0; h < 2 && !kPre; h++) {
                     uint32_t u = h ? uhi : ulo;
                     const uint64_t *rb = rows + ((int64_t)L * 64 + 32 * h) * W + lane;
                     while (u) {
@@ -1477,7 +1488,7 @@ __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
                 if (j >= R) break;
                 const unsigned long long t = pgd_warp_sum(__popcll(T[j]));
                 const unsigned long long nsq = pgd_warp_sum(__popcll(Sq[j]));
-                const unsigned long long k4 = pgd_warp_sum(k4x2[j]) >> 1;
+                const unsigned long long k4 = kPre ? A.k4pre[i0 + j] : pgd_warp_sum(k4x2[j]) >> 1;
                 // sum_{S_q} CN[p][w] - sum_T CN[q][x]: lane shares are signed, the
                 // warp's total modulo 2^64 is exact (|total| < 2^23)
                 const unsigned long long dtot = pgd_warp_sum((unsigned long long)(long long)dsum[j]);
@@ -1490,6 +1501,297 @@ __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
         }
     }
     block_flush(G, acc, cur_g, s_red, 8);
+}
+
+// ---------------------------------------------------------------------------
+// k4 of dense graphs on the tensor cores.  For an edge (p, q) with
+// T = N(p) ∩ N(q),
+//   2·k4(p, q) = sum_{y in T} |N(y) ∩ T| = sum_{y in N(q)} A_py · D[p][y],
+//   D[p][y]    = sum_{x in N(q)} A_px · A_yx = |N(p) ∩ N(y) ∩ N(q)|,
+// so for all edges (p_i, q) of one run (same q) D is a product of rows of the
+// ego network of q, compacted to the columns N(q): the rows p_i (M side, one
+// TMEM lane each) times every row y of N(q) (N side, one TMEM column each),
+// over K = N(q).  0/1 entries are exact in e4m3 and every fp32 sum stays below
+// 2^24 (d_q <= kTcMaxDeg), so the counts are exact.
+//
+// One CTA per SM takes runs from a counter.  Per run: the rows of N(q),
+// compacted to N(q)'s columns (a software bit-compress per 64-bit word, the
+// "compress" of Hacker's Delight §7-4 with its masks computed once per word of
+// A_q), go to shared memory; then per tile of 128 edges and 256 ego rows, each
+// 64-column chunk is expanded to e4m3 tiles in two alternating stages while
+// one thread issues the MMAs of the previous chunk; the accumulator is read
+// back per thread (row) and dotted with the row's own compact bits.
+
+constexpr int kTcThreads = 256;
+constexpr int kTcM = 128;                  // edges per tile (TMEM lanes)
+constexpr int kTcN = 256;                  // ego rows per tile (TMEM columns)
+constexpr int kTcK = 64;                   // ego columns per stage: one compact word
+constexpr int kTcMaxDeg = 1152;            // largest d_q whose compacted ego network fits shared memory
+constexpr int kTcMaxWords = kTcMaxDeg / 64;
+constexpr int kTcStageBytes = (kTcM + kTcN) * kTcK;
+constexpr int kTcSmem = 2 * kTcStageBytes + kTcMaxDeg * kTcMaxWords * 8 + 1024;
+constexpr long long kTcWaitCycles = 1ll << 30;   // about half a second: a wait that long has failed
+static_assert(kTcStageBytes % 1024 == 0, "stage tiles stay 1024-byte aligned");
+
+struct DenseTcArgs {
+    DevGraph G;
+    const uint64_t *bits;
+    const int64_t *wbase;
+    const int64_t *vbase;
+    const int32_t *dpos;                // positions of the CN-graph edges, grouped by q
+    const int64_t *runs;                // per run taken: {first, one past last} position
+    const unsigned long long *nruns;
+    uint32_t *k4;                       // per position: k4 (left at 0xffffffff outside the runs)
+    unsigned long long *next;
+    unsigned long long *err;            // waits that ran out
+};
+
+// run starts of the CN-graph edges (keys sorted: q in bits 32-62) whose q has
+// degree in [min_deg, kTcMaxDeg]
+__global__ void k_tc_run_flags(const uint64_t *keys, int64_t ncn, const int32_t *deg, int min_deg, uint32_t *flag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ncn; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t q = (uint32_t)(keys[i] >> 32) & 0x7fffffffu;
+        const bool start = i == 0 || ((uint32_t)(keys[i - 1] >> 32) & 0x7fffffffu) != q;
+        const int d = deg[q];
+        flag[i] = (start && d >= min_deg && d <= kTcMaxDeg) ? 1u : 0u;
+    }
+}
+
+__global__ void k_tc_run_fill(const uint64_t *keys, const uint32_t *flag, const uint32_t *pos, int64_t ncn,
+                              int64_t *runs, unsigned long long *nruns) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ncn; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!flag[i]) continue;
+        const uint32_t q = (uint32_t)(keys[i] >> 32) & 0x7fffffffu;
+        int64_t lo = i + 1, hi = ncn;   // one past the run's last position
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (((uint32_t)(keys[mid] >> 32) & 0x7fffffffu) == q) lo = mid + 1; else hi = mid;
+        }
+        runs[2 * pos[i]] = i;
+        runs[2 * pos[i] + 1] = lo;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *nruns = pos[ncn];
+}
+
+// masks of the compress of Hacker's Delight §7-4 (bits of x at the set bits of
+// m, packed to the low end), for repeated use with one m
+__device__ __forceinline__ void tc_compress_masks(uint64_t m, uint64_t mv[6]) {
+    uint64_t mk = ~m << 1;
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+        uint64_t mp = mk ^ (mk << 1);
+        mp ^= mp << 2;
+        mp ^= mp << 4;
+        mp ^= mp << 8;
+        mp ^= mp << 16;
+        mp ^= mp << 32;
+        const uint64_t v = mp & m;
+        mv[i] = v;
+        m = (m ^ v) | (v >> (1 << i));
+        mk &= ~mp;
+    }
+}
+
+__device__ __forceinline__ uint64_t tc_compress(uint64_t x, uint64_t m, const uint64_t mv[6]) {
+    x &= m;
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+        const uint64_t t = x & mv[i];
+        x = (x ^ t) | (t >> (1 << i));
+    }
+    return x;
+}
+
+// four bits -> four e4m3 bytes, 1.0 (0x38) where the bit is set
+__device__ __forceinline__ uint32_t tc_spread4(uint32_t nib) { return ((nib * 0x00204081u) & 0x01010101u) * 0x38u; }
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
+    extern __shared__ uint8_t tc_smem[];
+    __shared__ uint64_t s_m[32];          // A_q, per word
+    __shared__ uint64_t s_mv[32][6];      // compress masks per word of A_q
+    __shared__ int32_t s_o[33];           // compact offset of each word (prefix of popcounts)
+    __shared__ uint16_t s_col[kTcMaxDeg]; // N(q), ascending
+    __shared__ int16_t s_jrow[kTcM];      // compact row of each edge's p in the current tile, -1 past the run
+    __shared__ float s_part[2][kTcM];
+    __shared__ uint32_t s_taddr;
+    __shared__ __align__(8) uint64_t s_bar[2];
+    __shared__ long long s_run;
+    using namespace pgd_tc;
+    const DevGraph &G = A.G;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // 1024-aligned stages, then the compacted ego rows
+    uint8_t *base = tc_smem + ((1024u - (smem_addr(tc_smem) & 1023u)) & 1023u);
+    uint64_t *C = (uint64_t *)(base + 2 * kTcStageBytes);
+    if (warp == 0) tmem_alloc(&s_taddr, kTcN);
+    if (tid == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = s_taddr;
+    const uint32_t tlane = (uint32_t)(32 * (warp & 3)) << 16;   // this warp's TMEM lanes
+    uint32_t phase = 0, pend = 0;   // per stage: parity of its next phase, commit outstanding
+    int chunk = 0;
+    bool bad = false;
+    const int64_t nruns = (int64_t)*A.nruns;
+    while (true) {
+        if (tid == 0) s_run = (long long)atomicAdd(A.next, 1ull);
+        __syncthreads();
+        const int64_t r = s_run;
+        __syncthreads();
+        if (r >= nruns) break;
+        const int64_t i0 = A.runs[2 * r], i1 = A.runs[2 * r + 1];
+        const int32_t qg = dense_q(G, A.dpos[i0]);
+        const int g = G.egraph[A.dpos[i0]];
+        const int64_t vb = A.vbase[g];
+        const int W = (int)((G.gnm[2 * g] + 63) >> 6);
+        const uint64_t *rows = A.bits + A.wbase[g];
+        const int64_t q = qg - vb;
+        if (warp == 0) {
+            const uint64_t mq = lane < W ? __ldg(rows + q * W + lane) : 0ull;
+            const int c = __popcll(mq);
+            int o = c;
+#pragma unroll
+            for (int sft = 1; sft < 32; sft <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, o, sft);
+                if (lane >= sft) o += y;
+            }
+            o -= c;
+            s_m[lane] = mq;
+            s_o[lane] = o;
+            if (lane == 31) s_o[32] = o + c;
+            uint64_t mv[6];
+            tc_compress_masks(mq, mv);
+#pragma unroll
+            for (int i = 0; i < 6; i++) s_mv[lane][i] = mv[i];
+            uint64_t b = mq;
+            for (int j = o; b; j++) {
+                const int t = __ffsll(b) - 1;
+                b &= b - 1;
+                if (j < kTcMaxDeg) s_col[j] = (uint16_t)(64 * lane + t);
+            }
+        }
+        __syncthreads();
+        const int d = s_o[32];   // = deg(q), which the run flags bound; a run beyond the
+        if (d > kTcMaxDeg) continue;   // shared-memory limit is left to k_dense_cn
+        const int KW = (d + 63) >> 6;
+        for (int i = tid; i < d * KW; i += kTcThreads) C[i] = 0ull;
+        __syncthreads();
+        {   // C[j] = compact(A_{col[j]}), lane = word of the uncompacted row
+            uint64_t mv[6];
+#pragma unroll
+            for (int i = 0; i < 6; i++) mv[i] = s_mv[lane][i];
+            const uint64_t mw = s_m[lane];
+            const int ow = s_o[lane], cw = __popcll(mw), sh = ow & 63, w0 = ow >> 6;
+            for (int j = warp; j < d; j += kTcThreads / 32) {
+                const int x = s_col[j];
+                if (cw) {
+                    const uint64_t v = tc_compress(__ldg(rows + (int64_t)x * W + lane), mw, mv);
+                    if (v) {
+                        atomicOr((unsigned long long *)&C[j * KW + w0], (unsigned long long)(v << sh));
+                        if (sh && sh + cw > 64)
+                            atomicOr((unsigned long long *)&C[j * KW + w0 + 1], (unsigned long long)(v >> (64 - sh)));
+                    }
+                }
+            }
+        }
+        const int rr = (int)(i1 - i0);
+        for (int m0 = 0; m0 < rr && !bad; m0 += kTcM) {
+            __syncthreads();   // C complete; the previous tile's s_jrow and s_part read
+            if (tid < kTcM) {
+                int jr = -1;
+                if (m0 + tid < rr) {
+                    const int32_t id = G.order[A.dpos[i0 + m0 + tid]];
+                    const int32_t v = G.ev[id], u = G.eu[id];
+                    const int p = (int)((v == qg ? u : v) - vb);
+                    jr = s_o[p >> 6] + __popcll(s_m[p >> 6] & ((1ull << (p & 63)) - 1));
+                }
+                s_jrow[tid] = (int16_t)jr;
+            }
+            __syncthreads();
+            float acc = 0.f;   // row 32·(warp & 3) + lane of the tile, column half warp >> 2
+            for (int n0 = 0; n0 < d && !bad; n0 += kTcN) {
+                const int nt = min(kTcN, ((d - n0 + 15) >> 4) << 4);
+                const uint32_t idesc = idesc_e4m3_f32(kTcM, nt);
+                for (int kc = 0; kc < KW; kc++) {
+                    const int st = chunk & 1;
+                    if ((pend >> st) & 1u) {   // the MMAs that read this stage are done
+                        bad |= !mbar_wait(&s_bar[st], (phase >> st) & 1u, kTcWaitCycles);
+                        phase ^= 1u << st;
+                        pend &= ~(1u << st);
+                    }
+                    uint8_t *sA = base + st * kTcStageBytes, *sB = sA + kTcM * kTcK;
+                    // item it: 16 columns of one row; in the core-matrix layout
+                    // (LBO 128, SBO 512) item it lives at byte 16·it of its tile
+                    for (int it = tid; it < (kTcM + nt) * 4; it += kTcThreads) {
+                        const bool isA = it < kTcM * 4;
+                        const int i2 = isA ? it : it - kTcM * 4;
+                        const int cm = i2 >> 3, row = (cm >> 2) * 8 + (i2 & 7), blk = cm & 3;
+                        const int cr = isA ? s_jrow[row] : (n0 + row < d ? n0 + row : -1);
+                        const uint32_t b16 = cr >= 0 ? (uint32_t)(C[cr * KW + kc] >> (16 * blk)) & 0xffffu : 0u;
+                        *(uint4 *)((isA ? sA : sB) + (size_t)i2 * 16) =
+                            make_uint4(tc_spread4(b16 & 15u), tc_spread4((b16 >> 4) & 15u),
+                                       tc_spread4((b16 >> 8) & 15u), tc_spread4(b16 >> 12));
+                    }
+                    fence_async_smem();
+                    if (__syncthreads_or(bad)) {
+                        bad = true;
+                        break;
+                    }
+                    if (tid == 0) {
+                        fence_after_sync();
+#pragma unroll
+                        for (int ks = 0; ks < 2; ks++)
+                            mma_e4m3(tmem, smem_desc(smem_addr(sA) + 256 * ks, 128, 512),
+                                     smem_desc(smem_addr(sB) + 256 * ks, 128, 512), idesc, (kc | ks) != 0);
+                        mma_commit(&s_bar[st]);
+                    }
+                    pend |= 1u << st;
+                    chunk++;
+                }
+                // the accumulator is complete once both stages' last commits land
+                for (int st = 0; st < 2; st++)
+                    if ((pend >> st) & 1u) {
+                        bad |= !mbar_wait(&s_bar[st], (phase >> st) & 1u, kTcWaitCycles);
+                        phase ^= 1u << st;
+                        pend &= ~(1u << st);
+                    }
+                if (__syncthreads_or(bad)) {
+                    bad = true;
+                    break;
+                }
+                fence_after_sync();
+                const int row = 32 * (warp & 3) + lane, h = warp >> 2;
+                const int jr = s_jrow[row];
+                const int cend = min(nt, h * 128 + 128);
+                for (int c0 = h * 128; c0 < cend; c0 += 16) {
+                    uint32_t v[16];
+                    tmem_ld16(tmem + tlane + (uint32_t)c0, v);
+                    const int y0 = n0 + c0;   // a multiple of 16, below d
+                    const uint32_t b16 = jr >= 0 ? (uint32_t)(C[jr * KW + (y0 >> 6)] >> (y0 & 63)) & 0xffffu : 0u;
+#pragma unroll
+                    for (int i = 0; i < 16; i++) acc += ((b16 >> i) & 1u) ? __uint_as_float(v[i]) : 0.f;
+                }
+                fence_before_sync();
+                __syncthreads();   // accumulator read before the next tile's MMAs
+            }
+            if (bad) break;
+            s_part[warp >> 2][32 * (warp & 3) + lane] = acc;
+            __syncthreads();
+            if (tid < kTcM && m0 + tid < rr) A.k4[i0 + m0 + tid] = (uint32_t)(s_part[0][tid] + s_part[1][tid]) >> 1;
+        }
+        if (bad) break;
+    }
+    if (bad) {
+        if (tid == 0) atomicAdd(A.err, 1ull);
+        for (int st = 0; st < 2; st++)   // MMAs still in flight: one more bounded wait each
+            if ((pend >> st) & 1u) mbar_wait(&s_bar[st], (phase >> st) & 1u, kTcWaitCycles);
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, kTcN);
 }
 
 }  // namespace
@@ -1675,6 +1977,51 @@ struct DenseView {
     const int64_t *cbase;     // per graph: first CN entry, or -1
 };
 
+// k4 of the CN-graph edges whose q has degree in [ctx->tc_min_deg, kTcMaxDeg],
+// on the tensor cores (k_dense_tc): runs of equal q from the sorted dense
+// keys, then one CTA per SM.  *k4_out gets k4 per position of dpos
+// (0xffffffff outside those runs); ctr[8..10] are its run counter, run count
+// and failed-wait count, ctr[11] the counter of k_dense_cn<true>.
+static pgd_status dense_tc(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, const DenseView *dense,
+                           const int32_t *dpos, const uint64_t *keys, int64_t ncn, uint32_t **k4_out) {
+    cudaStream_t s = ctx->stream;
+    pgd_status st;
+    uint32_t *flag = nullptr, *pos = nullptr, *k4 = nullptr;
+    int64_t *runs = nullptr;
+    const int64_t maxruns = std::min<int64_t>(ncn, G.n);
+    if ((st = tg.alloc(&flag, (ncn + 1) * sizeof(uint32_t)))) return st;
+    if ((st = tg.alloc(&pos, (ncn + 1) * sizeof(uint32_t)))) return st;
+    if ((st = tg.alloc(&k4, ncn * sizeof(uint32_t)))) return st;
+    if ((st = tg.alloc(&runs, (2 * maxruns + 2) * sizeof(int64_t)))) return st;
+    unsigned long long *ctr = ctx->d_ctr;
+    PGD_CUDA(ctx, cudaMemsetAsync(ctr + 8, 0, 4 * sizeof(unsigned long long), s));
+    PGD_LAUNCH(ctx, k_tc_run_flags, grid_for(ncn), kThreads, 0, keys, ncn, G.deg, ctx->tc_min_deg, flag);
+    PGD_CUDA(ctx, cudaMemsetAsync(flag + ncn, 0, sizeof(uint32_t), s));
+    size_t tb = 0;
+    void *tmp = nullptr;
+    cub::DeviceScan::ExclusiveSum(nullptr, tb, flag, pos, ncn + 1, s);
+    if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
+    cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, ncn + 1, s);
+    pgd_tmp_free(ctx, tmp);
+    PGD_LAUNCH(ctx, k_tc_run_fill, grid_for(ncn), kThreads, 0, keys, flag, pos, ncn, runs, ctr + 9);
+    PGD_CUDA(ctx, cudaMemsetAsync(k4, 0xff, ncn * sizeof(uint32_t), s));
+    PGD_CUDA(ctx, cudaFuncSetAttribute(k_dense_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+    DenseTcArgs T;
+    T.G = G;
+    T.bits = dense->bits;
+    T.wbase = dense->wbase;
+    T.vbase = dense->vbase;
+    T.dpos = dpos;
+    T.runs = runs;
+    T.nruns = ctr + 9;
+    T.k4 = k4;
+    T.next = ctr + 8;
+    T.err = ctr + 10;
+    PGD_LAUNCH(ctx, k_dense_tc, ctx->num_sms, kTcThreads, kTcSmem, T);
+    *k4_out = k4;
+    return PGD_OK;
+}
+
 // Where k_hub keeps the W histogram and the N(p) rank bitmap: the histogram
 // (atomics) in shared memory when it fits, then as many bitmap ranks as the
 // remaining shared memory holds; per-CTA global slices for the rest.  Fills
@@ -1813,6 +2160,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     int32_t *thigh = nullptr;
     TmpGuard tg(ctx);
     const int nsm = ctx->num_sms;
+    bool tc_ran = false;
     HubArgs H;
     const size_t smem = hub_layout(G.n, nhubs, nwide, max_degree, &H);
     if ((int64_t)H.split < G.n) {
@@ -1897,6 +2245,11 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
             PGD_CUDA(ctx, cudaStreamSynchronize(s));
             ncn = (int64_t)h;
         }
+        uint32_t *k4pre = nullptr;
+        if (ncn > 0 && ctx->tc_min_deg > 0) {
+            if ((st = dense_tc(ctx, G, tg, dense, posv + nh, keys2, ncn, &k4pre))) return st;
+            tc_ran = true;
+        }
         if (ncn > 0) {
             DenseCnArgs C;
             C.G = G;
@@ -1906,9 +2259,14 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
             C.cn = dense->cn;
             C.cbase = dense->cbase;
             C.dpos = posv + nh;
+            C.k4pre = k4pre;
             C.ndense = ncn;
             C.next = ctr + 6;
-            PGD_LAUNCH(ctx, k_dense_cn, nsm * 8, 256, 0, C);
+            PGD_LAUNCH(ctx, k_dense_cn<false>, nsm * 8, 256, 0, C);
+            if (k4pre) {
+                C.next = ctr + 11;
+                PGD_LAUNCH(ctx, k_dense_cn<true>, nsm * 8, 256, 0, C);
+            }
         }
         if ((int64_t)nd > ncn) {
             DenseArgs D;
@@ -1936,6 +2294,11 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     PGD_CUDA(ctx, cudaEventElapsedTime(&ms->total, ctx->ev0, ctx->ev1));
     PGD_CUDA(ctx, cudaEventElapsedTime(&ms->tri, ctx->evt0, ctx->evt1));
     if (nitems > 0) PGD_CUDA(ctx, cudaEventElapsedTime(&ms->hub, ctx->evh0, ctx->evh1));
+    if (tc_ran) {
+        unsigned long long failed = 0;
+        PGD_CUDA(ctx, cudaMemcpy(&failed, ctr + 10, sizeof(failed), cudaMemcpyDeviceToHost));
+        if (failed) return pgd_fail(ctx, PGD_ETIMEOUT, "a tensor-core wait in k_dense_tc ran out");
+    }
     return PGD_OK;
 }
 
