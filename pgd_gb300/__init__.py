@@ -266,7 +266,7 @@ class Context:
         return a.value, c.value, d.value
 
     def set_tensor_min_degree(self, d):
-        """Dense batch graphs: runs with q of degree in [d, 1152] count k4 on the tensor cores (0: never)."""
+        """Dense batch graphs: runs with q of degree in [d, 1088] count k4 on the tensor cores (0: never)."""
         self._check(lib().pgd_set_tensor_min_degree(self.h, d), "pgd_set_tensor_min_degree")
 
     def tensor_min_degree(self):

@@ -447,8 +447,8 @@ extern "C" pgd_status pgd_get_thresholds(const pgd_ctx *ctx, int *anchor_hub, in
 
 extern "C" pgd_status pgd_set_tensor_min_degree(pgd_ctx *ctx, int tensor_min_degree) {
     if (!ctx) return PGD_EINVAL;
-    if (tensor_min_degree != 0 && (tensor_min_degree < 2 || tensor_min_degree > 1152))
-        return pgd_fail(ctx, PGD_EINVAL, "tensor_min_degree out of range (0, or 2..1152)");
+    if (tensor_min_degree != 0 && (tensor_min_degree < 2 || tensor_min_degree > 1088))
+        return pgd_fail(ctx, PGD_EINVAL, "tensor_min_degree out of range (0, or 2..1088)");
     ctx->tc_min_deg = tensor_min_degree;
     return PGD_OK;
 }

@@ -1514,24 +1514,30 @@ __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
 // over K = N(q).  0/1 entries are exact in e4m3 and every fp32 sum stays below
 // 2^24 (d_q <= kTcMaxDeg), so the counts are exact.
 //
-// One CTA per SM takes runs from a counter.  Per run: the rows of N(q),
-// compacted to N(q)'s columns (a software bit-compress per 64-bit word, the
-// "compress" of Hacker's Delight §7-4 with its masks computed once per word of
-// A_q), go to shared memory; then per tile of 128 edges and 256 ego rows, each
-// 64-column chunk is expanded to e4m3 tiles in two alternating stages while
-// one thread issues the MMAs of the previous chunk; the accumulator is read
-// back per thread (row) and dotted with the row's own compact bits.
+// One CTA of 16 warps per SM takes runs from a counter.  Per run: the rows of
+// N(q), compacted to N(q)'s columns (a software bit-compress per 64-bit word,
+// the "compress" of Hacker's Delight §7-4 with its masks computed once per word
+// of A_q), go to shared memory.  Then for each pair of 128-edge tiles and each
+// 256-row tile of N(q), every 64-column chunk is expanded to e4m3 tiles (one B
+// tile shared by both edge tiles) in one of two alternating stages while the
+// tensor cores run the previous chunk's MMAs, which one thread issues into two
+// TMEM accumulators; at the end of a row tile every warp reads back one
+// accumulator quarter (a row per thread) and dots it with the rows' own
+// compact bits.  A one is encoded as 2^-6 (0x08), so that a nibble spreads to
+// four bytes in two instructions; all sums are multiples of 2^-12 below 2^9,
+// exact in fp32.
 
-constexpr int kTcThreads = 256;
-constexpr int kTcM = 128;                  // edges per tile (TMEM lanes)
-constexpr int kTcN = 256;                  // ego rows per tile (TMEM columns)
+constexpr int kTcThreads = 512;
+constexpr int kTcM = 128;                  // edges per tile (TMEM lanes); two tiles per pass
+constexpr int kTcN = 256;                  // ego rows per tile (TMEM columns per accumulator)
 constexpr int kTcK = 64;                   // ego columns per stage: one compact word
-constexpr int kTcMaxDeg = 1152;            // largest d_q whose compacted ego network fits shared memory
+constexpr int kTcMaxDeg = 1088;            // largest d_q whose compacted ego network fits shared memory
 constexpr int kTcMaxWords = kTcMaxDeg / 64;
-constexpr int kTcStageBytes = (kTcM + kTcN) * kTcK;
+constexpr int kTcStageBytes = (2 * kTcM + kTcN) * kTcK;   // A tiles of both edge tiles, then B
 constexpr int kTcSmem = 2 * kTcStageBytes + kTcMaxDeg * kTcMaxWords * 8 + 1024;
 constexpr long long kTcWaitCycles = 1ll << 30;   // about half a second: a wait that long has failed
 static_assert(kTcStageBytes % 1024 == 0, "stage tiles stay 1024-byte aligned");
+static_assert(kTcMaxDeg % 64 == 0, "whole compact words");
 
 struct DenseTcArgs {
     DevGraph G;
@@ -1602,8 +1608,9 @@ __device__ __forceinline__ uint64_t tc_compress(uint64_t x, uint64_t m, const ui
     return x;
 }
 
-// four bits -> four e4m3 bytes, 1.0 (0x38) where the bit is set
-__device__ __forceinline__ uint32_t tc_spread4(uint32_t nib) { return ((nib * 0x00204081u) & 0x01010101u) * 0x38u; }
+// four bits -> four e4m3 bytes, 2^-6 (0x08) where the bit is set: the
+// product places bit i of nib at bit 8i + 3, and no two shifted copies overlap
+__device__ __forceinline__ uint32_t tc_spread4(uint32_t nib) { return (nib * 0x01020408u) & 0x08080808u; }
 
 __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
     extern __shared__ uint8_t tc_smem[];
@@ -1611,8 +1618,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
     __shared__ uint64_t s_mv[32][6];      // compress masks per word of A_q
     __shared__ int32_t s_o[33];           // compact offset of each word (prefix of popcounts)
     __shared__ uint16_t s_col[kTcMaxDeg]; // N(q), ascending
-    __shared__ int16_t s_jrow[kTcM];      // compact row of each edge's p in the current tile, -1 past the run
-    __shared__ float s_part[2][kTcM];
+    __shared__ int16_t s_jrow[2][kTcM];   // compact row of each edge's p in the pass, -1 past the run
+    __shared__ float s_part[2][2][kTcM];  // per edge tile and column half
     __shared__ uint32_t s_taddr;
     __shared__ __align__(8) uint64_t s_bar[2];
     __shared__ long long s_run;
@@ -1622,7 +1629,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
     // 1024-aligned stages, then the compacted ego rows
     uint8_t *base = tc_smem + ((1024u - (smem_addr(tc_smem) & 1023u)) & 1023u);
     uint64_t *C = (uint64_t *)(base + 2 * kTcStageBytes);
-    if (warp == 0) tmem_alloc(&s_taddr, kTcN);
+    if (warp == 0) tmem_alloc(&s_taddr, 2 * kTcN);
     if (tid == 0) {
         mbar_init(&s_bar[0], 1);
         mbar_init(&s_bar[1], 1);
@@ -1631,8 +1638,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = s_taddr;
-    const uint32_t tlane = (uint32_t)(32 * (warp & 3)) << 16;   // this warp's TMEM lanes
-    uint32_t phase = 0, pend = 0;   // per stage: parity of its next phase, commit outstanding
+    // read-back role: edge tile et, column half eh, TMEM lanes 32·(warp & 3)
+    const int et = warp >> 3, eh = (warp >> 2) & 1, erow = 32 * (warp & 3) + lane;
+    const uint32_t etaddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(et * kTcN);
+    uint32_t phase = 0, pend = 0;   // thread 0, per stage: parity of its next phase, commit outstanding
     int chunk = 0;
     bool bad = false;
     const int64_t nruns = (int64_t)*A.nruns;
@@ -1698,9 +1707,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
             }
         }
         const int rr = (int)(i1 - i0);
-        for (int m0 = 0; m0 < rr && !bad; m0 += kTcM) {
-            __syncthreads();   // C complete; the previous tile's s_jrow and s_part read
-            if (tid < kTcM) {
+        for (int m0 = 0; m0 < rr && !bad; m0 += 2 * kTcM) {
+            const int ntiles = rr - m0 > kTcM ? 2 : 1;   // edge tiles of this pass
+            __syncthreads();   // C complete; the previous pass's s_jrow and s_part read
+            if (tid < 2 * kTcM) {
                 int jr = -1;
                 if (m0 + tid < rr) {
                     const int32_t id = G.order[A.dpos[i0 + m0 + tid]];
@@ -1708,90 +1718,121 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
                     const int p = (int)((v == qg ? u : v) - vb);
                     jr = s_o[p >> 6] + __popcll(s_m[p >> 6] & ((1ull << (p & 63)) - 1));
                 }
-                s_jrow[tid] = (int16_t)jr;
+                s_jrow[tid >> 7][tid & (kTcM - 1)] = (int16_t)jr;
             }
             __syncthreads();
-            float acc = 0.f;   // row 32·(warp & 3) + lane of the tile, column half warp >> 2
+            float acc = 0.f;   // row erow of edge tile et, column half eh
             for (int n0 = 0; n0 < d && !bad; n0 += kTcN) {
                 const int nt = min(kTcN, ((d - n0 + 15) >> 4) << 4);
                 const uint32_t idesc = idesc_e4m3_f32(kTcM, nt);
+                // this thread's items (16 columns of one row each) of every
+                // chunk of this tile: compact source word, shift, destination.
+                // In the core-matrix layout (LBO 128, SBO 512) item i of a tile
+                // lives at byte 16·i; a stage holds A of tile 0, A of tile 1, B.
+                const int nA = ntiles * kTcM * 4, nItems = nA + nt * 4;
+                int src[4], shf[4];
+                uint32_t dst[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int it = tid + k * kTcThreads;
+                    const bool isA = it < nA;
+                    const int i2 = isA ? (it & (kTcM * 4 - 1)) : it - nA;
+                    const int row = ((i2 >> 5) << 3) | (i2 & 7);
+                    int cr = -1;
+                    if (it < nItems) cr = isA ? s_jrow[it >> 9][row] : (n0 + row < d ? n0 + row : -1);
+                    src[k] = cr >= 0 ? cr * KW : -1;
+                    shf[k] = 16 * ((i2 >> 3) & 3);
+                    dst[k] = isA ? (uint32_t)((it >> 9) * kTcM * kTcK + 16 * i2) : (uint32_t)(2 * kTcM * kTcK + 16 * i2);
+                }
                 for (int kc = 0; kc < KW; kc++) {
                     const int st = chunk & 1;
-                    if ((pend >> st) & 1u) {   // the MMAs that read this stage are done
-                        bad |= !mbar_wait(&s_bar[st], (phase >> st) & 1u, kTcWaitCycles);
-                        phase ^= 1u << st;
-                        pend &= ~(1u << st);
-                    }
-                    uint8_t *sA = base + st * kTcStageBytes, *sB = sA + kTcM * kTcK;
-                    // item it: 16 columns of one row; in the core-matrix layout
-                    // (LBO 128, SBO 512) item it lives at byte 16·it of its tile
-                    for (int it = tid; it < (kTcM + nt) * 4; it += kTcThreads) {
-                        const bool isA = it < kTcM * 4;
-                        const int i2 = isA ? it : it - kTcM * 4;
-                        const int cm = i2 >> 3, row = (cm >> 2) * 8 + (i2 & 7), blk = cm & 3;
-                        const int cr = isA ? s_jrow[row] : (n0 + row < d ? n0 + row : -1);
-                        const uint32_t b16 = cr >= 0 ? (uint32_t)(C[cr * KW + kc] >> (16 * blk)) & 0xffffu : 0u;
-                        *(uint4 *)((isA ? sA : sB) + (size_t)i2 * 16) =
-                            make_uint4(tc_spread4(b16 & 15u), tc_spread4((b16 >> 4) & 15u),
-                                       tc_spread4((b16 >> 8) & 15u), tc_spread4(b16 >> 12));
+                    uint8_t *stg = base + st * kTcStageBytes;
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        if (tid + k * kTcThreads < nItems) {
+                            const uint32_t b16 = src[k] >= 0 ? (uint32_t)(C[src[k] + kc] >> shf[k]) & 0xffffu : 0u;
+                            *(uint4 *)(stg + dst[k]) =
+                                make_uint4(tc_spread4(b16 & 15u), tc_spread4((b16 >> 4) & 15u),
+                                           tc_spread4((b16 >> 8) & 15u), tc_spread4(b16 >> 12));
+                        }
                     }
                     fence_async_smem();
+                    __syncthreads();   // stage st written
+                    if (tid == 0) {
+                        fence_after_sync();
+                        const uint32_t sa = smem_addr(stg), sb = sa + 2 * kTcM * kTcK;
+                        for (int t = 0; t < ntiles; t++)
+#pragma unroll
+                            for (int ks = 0; ks < 2; ks++)
+                                mma_e4m3(tmem + (uint32_t)(t * kTcN), smem_desc(sa + t * kTcM * kTcK + 256 * ks, 128, 512),
+                                         smem_desc(sb + 256 * ks, 128, 512), idesc, (kc | ks) != 0);
+                        mma_commit(&s_bar[st]);
+                        pend |= 1u << st;
+                        // the next chunk overwrites the other stage: its MMAs must be done
+                        if ((pend >> (st ^ 1)) & 1u) {
+                            bad |= !mbar_wait(&s_bar[st ^ 1], (phase >> (st ^ 1)) & 1u, kTcWaitCycles);
+                            phase ^= 1u << (st ^ 1);
+                            pend &= ~(1u << (st ^ 1));
+                        }
+                    }
+                    chunk++;
                     if (__syncthreads_or(bad)) {
                         bad = true;
                         break;
                     }
-                    if (tid == 0) {
-                        fence_after_sync();
-#pragma unroll
-                        for (int ks = 0; ks < 2; ks++)
-                            mma_e4m3(tmem, smem_desc(smem_addr(sA) + 256 * ks, 128, 512),
-                                     smem_desc(smem_addr(sB) + 256 * ks, 128, 512), idesc, (kc | ks) != 0);
-                        mma_commit(&s_bar[st]);
-                    }
-                    pend |= 1u << st;
-                    chunk++;
                 }
-                // the accumulator is complete once both stages' last commits land
-                for (int st = 0; st < 2; st++)
-                    if ((pend >> st) & 1u) {
-                        bad |= !mbar_wait(&s_bar[st], (phase >> st) & 1u, kTcWaitCycles);
-                        phase ^= 1u << st;
-                        pend &= ~(1u << st);
-                    }
+                if (bad) break;
+                // the accumulators are complete once the last commits land
+                if (tid == 0)
+                    for (int st = 0; st < 2; st++)
+                        if ((pend >> st) & 1u) {
+                            bad |= !mbar_wait(&s_bar[st], (phase >> st) & 1u, kTcWaitCycles);
+                            phase ^= 1u << st;
+                            pend &= ~(1u << st);
+                        }
                 if (__syncthreads_or(bad)) {
                     bad = true;
                     break;
                 }
                 fence_after_sync();
-                const int row = 32 * (warp & 3) + lane, h = warp >> 2;
-                const int jr = s_jrow[row];
-                const int cend = min(nt, h * 128 + 128);
-                for (int c0 = h * 128; c0 < cend; c0 += 16) {
-                    uint32_t v[16];
-                    tmem_ld16(tmem + tlane + (uint32_t)c0, v);
-                    const int y0 = n0 + c0;   // a multiple of 16, below d
-                    const uint32_t b16 = jr >= 0 ? (uint32_t)(C[jr * KW + (y0 >> 6)] >> (y0 & 63)) & 0xffffu : 0u;
+                if (et < ntiles) {
+                    const int jr = s_jrow[et][erow];
+                    const int cend = min(nt, eh * 128 + 128);
+                    for (int c0 = eh * 128; c0 < cend; c0 += 16) {
+                        uint32_t v[16];
+                        tmem_ld16(etaddr + (uint32_t)c0, v);
+                        const int y0 = n0 + c0;   // a multiple of 16, below d
+                        const uint32_t b16 =
+                            jr >= 0 ? (uint32_t)(C[jr * KW + (y0 >> 6)] >> (y0 & 63)) & 0xffffu : 0u;
 #pragma unroll
-                    for (int i = 0; i < 16; i++) acc += ((b16 >> i) & 1u) ? __uint_as_float(v[i]) : 0.f;
+                        for (int i = 0; i < 16; i++) acc += ((b16 >> i) & 1u) ? __uint_as_float(v[i]) : 0.f;
+                    }
                 }
                 fence_before_sync();
-                __syncthreads();   // accumulator read before the next tile's MMAs
+                __syncthreads();   // accumulators read before the next tile's MMAs
             }
             if (bad) break;
-            s_part[warp >> 2][32 * (warp & 3) + lane] = acc;
+            if (et < ntiles) s_part[et][eh][erow] = acc;
             __syncthreads();
-            if (tid < kTcM && m0 + tid < rr) A.k4[i0 + m0 + tid] = (uint32_t)(s_part[0][tid] + s_part[1][tid]) >> 1;
+            if (tid < ntiles * kTcM && m0 + tid < rr) {
+                const int t = tid >> 7, row = tid & (kTcM - 1);
+                // (sum of D·A_py) · 2^12 = 2·k4
+                const float k2 = (s_part[t][0][row] + s_part[t][1][row]) * 4096.f;
+                A.k4[i0 + m0 + tid] = (uint32_t)k2 >> 1;
+            }
         }
         if (bad) break;
     }
     if (bad) {
-        if (tid == 0) atomicAdd(A.err, 1ull);
-        for (int st = 0; st < 2; st++)   // MMAs still in flight: one more bounded wait each
-            if ((pend >> st) & 1u) mbar_wait(&s_bar[st], (phase >> st) & 1u, kTcWaitCycles);
+        if (tid == 0) {
+            atomicAdd(A.err, 1ull);
+            for (int st = 0; st < 2; st++)   // MMAs still in flight: one more bounded wait each
+                if ((pend >> st) & 1u) mbar_wait(&s_bar[st], (phase >> st) & 1u, kTcWaitCycles);
+        }
     }
     fence_before_sync();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, kTcN);
+    if (warp == 0) tmem_dealloc(tmem, 2 * kTcN);
 }
 
 }  // namespace

@@ -1,5 +1,5 @@
 """4-cliques of dense batch graphs on the tensor cores (k_dense_tc): for the
-runs of edges sharing q whose degree lies in [tensor_min_degree, 1152], k4
+runs of edges sharing q whose degree lies in [tensor_min_degree, 1088], k4
 comes from an e4m3 product of q's ego network accumulated in TMEM.  Counts
 must not depend on which runs take that path: every per-edge row and total
 equals the integer path's (tensor_min_degree 0), the single-graph kernels',
@@ -14,9 +14,9 @@ pytestmark = pytest.mark.gpu
 
 # d_q across the path's limits: below and above 128 (default threshold),
 # runs of more than 128 edges (several M tiles), d_q above 256 (several N
-# tiles), d_q not a multiple of 16 or 64, and d_q around 1152 (the largest
-# ego network the kernel keeps in shared memory) in (1300, 0.885)
-SPECS = [(1300, 0.885), (2048, 0.5), (600, 0.5), (257, 0.99), (1200, 0.11), (160, 0.85), (900, 0.3),
+# tiles), d_q not a multiple of 16 or 64, and d_q around 1088 (the largest
+# ego network the kernel keeps in shared memory) in (1230, 0.885)
+SPECS = [(1230, 0.885), (2048, 0.5), (600, 0.5), (257, 0.99), (1200, 0.11), (160, 0.85), (900, 0.3),
          (40, 0.9), (2000, 0.07)]
 
 
@@ -52,11 +52,11 @@ def test_tensor_k4_equals_integer_path_and_single_graph():
         g.preprocess("deg")
         g.sort_edges("kcore")
     degs = [g.info().max_degree for g in graphs]
-    assert max(degs) > 1152 and any(128 <= d <= 1152 for d in degs)
+    assert max(degs) > 1088 and any(128 <= d <= 1088 for d in degs)
     c.set_tensor_min_degree(0)
     assert c.tensor_min_degree() == 0
     base, base_rows = batch_rows(c, graphs)
-    for tmin in (2, 128, 1152):
+    for tmin in (2, 128, 1088):
         c.set_tensor_min_degree(tmin)
         res, rows = batch_rows(c, graphs)
         for i in range(len(graphs)):
@@ -113,10 +113,10 @@ def test_tensor_k4_oracle(n, p, seed):
 
 def test_tensor_min_degree_range():
     c = pgd.Context()
-    for bad in (1, -1, 1153):
+    for bad in (1, -1, 1089):
         with pytest.raises(pgd.PGDError) as e:
             c.set_tensor_min_degree(bad)
         assert e.value.status == 1
-    c.set_tensor_min_degree(1152)
-    assert c.tensor_min_degree() == 1152
+    c.set_tensor_min_degree(1088)
+    assert c.tensor_min_degree() == 1088
     c.close()
