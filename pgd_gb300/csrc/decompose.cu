@@ -1363,6 +1363,7 @@ struct DenseCnArgs {
     const int64_t *cbase;     // per graph: first entry of its CN matrix
     const int32_t *dpos;      // E_ordered positions of those graphs' edges, grouped by q
     const uint32_t *k4pre;    // per position of dpos: k4 from k_dense_tc, 0xffffffff where not taken (or null)
+    const int32_t *eslot;     // with k4pre: E[x][y] per adjacency slot x -> y, from k_dense_gram
     int64_t ndense;
     unsigned long long *next;
 };
@@ -1370,8 +1371,9 @@ struct DenseCnArgs {
 // Up to kDenseGroup edges (p_j, q) with the same q, as in k_dense; per row
 // word L of A_q the warp reads 64 entries of CN[q] and of each CN[p_j] (two
 // per lane) for the two sums, and the rows of the word's members of T_j.
-// kPre: only the groups whose k4 k_dense_tc counted (no scan of T's rows);
-// otherwise only the others.
+// kPre: only the groups whose k4 k_dense_tc counted; their two sums come
+// from E (k_dense_gram) as E[q][p] - d_p, so no row is scanned at all.
+// Otherwise only the other groups.
 template <bool kPre>
 __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
     __shared__ unsigned long long s_red[8][PGD_NSUMS];
@@ -1429,7 +1431,30 @@ __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
                     pl[j] = (int32_t)p;
                 }
             }
-            for (int L = 0; L < W; L++) {
+            unsigned long long dpre[kDenseGroup];   // kPre: E[q][p_j] - d_p (mod 2^64)
+            if constexpr (kPre) {
+                // rank of p_j in N(q): popcounts of A_q's words before p_j's, then of its word below it
+                const int c = __popcll(Aq);
+                int o = c;
+#pragma unroll
+                for (int sft = 1; sft < 32; sft <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, o, sft);
+                    if (lane >= sft) o += y;
+                }
+                o -= c;
+                const int64_t qoff = G.off[qg];
+#pragma unroll
+                for (int j = 0; j < kDenseGroup; j++) {
+                    dpre[j] = 0;
+                    if (j < R) {
+                        const int pw = pl[j] >> 6;
+                        const uint64_t below = __shfl_sync(0xffffffffu, Aq, pw) & ((1ull << (pl[j] & 63)) - 1);
+                        const int rank = __shfl_sync(0xffffffffu, o, pw) + __popcll(below);
+                        dpre[j] = (unsigned long long)(long long)(A.eslot[qoff + rank] - G.deg[vb + pl[j]]);
+                    }
+                }
+            }
+            for (int L = 0; L < W && !kPre; L++) {
                 // word L of every T_j as 32-bit halves
                 uint32_t tlo[kDenseGroup], thi[kDenseGroup];
                 uint32_t ulo = 0, uhi = 0;
@@ -1460,7 +1485,7 @@ __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
                 // rows of this word's members of the T_j (k4), one half at a
                 // time, two rows in flight, each row tested against every T_j
 #pragma unroll
-                for (int h = 0; h < 2 && !kPre; h++) {
+                for (int h = 0; h < 2; h++) {
                     uint32_t u = h ? uhi : ulo;
                     const uint64_t *rb = rows + ((int64_t)L * 64 + 32 * h) * W + lane;
                     while (u) {
@@ -1491,7 +1516,8 @@ __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
                 const unsigned long long k4 = kPre ? A.k4pre[i0 + j] : pgd_warp_sum(k4x2[j]) >> 1;
                 // sum_{S_q} CN[p][w] - sum_T CN[q][x]: lane shares are signed, the
                 // warp's total modulo 2^64 is exact (|total| < 2^23)
-                const unsigned long long dtot = pgd_warp_sum((unsigned long long)(long long)dsum[j]);
+                const unsigned long long dtot =
+                    kPre ? dpre[j] : pgd_warp_sum((unsigned long long)(long long)dsum[j]);
                 const unsigned long long c = dtot + 2 * k4 + t - nsq;
                 const int64_t e = A.dpos[i0 + j];
                 const int32_t id = G.order[e];
@@ -1835,6 +1861,212 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
     if (warp == 0) tmem_dealloc(tmem, 2 * kTcN);
 }
 
+// ---------------------------------------------------------------------------
+// The two c4 sums of a dense graph's edges on the tensor cores.  With A the
+// adjacency, CN = A² and TA = A ∘ CN (t of each edge, 0 off the edges), an
+// edge (p, q) with S_q = N(q) \ N(p) \ {p} and T = N(p) ∩ N(q) has
+//   sum_{w in S_q} CN[p][w] = (A·CN)[q][p] - (TA·A)[p][q] - d_p,
+//   sum_{x in T}   CN[q][x] = (TA·A)[q][p],
+// so their difference is E[q][p] - d_p with the symmetric integer matrix
+//   E = A·(CN - TA) - TA·A.
+// One CTA per SM takes (graph, 128-row tile, 256-column tile) items; each
+// item runs the chain over K = n of A × (CN - TA), then of TA × A with the
+// product negated, in tf32 (entries below 2^11 are exact, |sums| < 2^23 stay
+// exact in fp32), 16 columns per stage from four stages.  The tile is read
+// back one row per thread and E[x][y] written for the edges only, at the
+// adjacency slot x -> y.
+
+constexpr int kGramThreads = 512;
+constexpr int kGramM = 128, kGramN = 256;
+constexpr int kGramStages = 4;
+constexpr int kGramStageBytes = (kGramM + kGramN) * 64;   // 16 tf32 columns per row
+constexpr int kGramSmem = kGramStages * kGramStageBytes + 1024;
+static_assert(kGramStageBytes % 1024 == 0, "stage tiles stay 1024-byte aligned");
+
+struct GramArgs {
+    const uint64_t *bits;
+    const int64_t *wbase;
+    const int64_t *vbase;
+    const uint16_t *cn;
+    const int64_t *cbase;
+    const long long *gnm;
+    const int64_t *off;        // union adjacency offsets
+    const int64_t *etile;      // first item of each graph (k + 1 entries)
+    int k;
+    int32_t *eslot;            // E[x][y] per adjacency slot x -> y of the graphs with a CN matrix
+    unsigned long long *next;
+    unsigned long long *err;
+};
+
+__global__ void k_gram_tiles(const long long *gnm, const int64_t *cbase, int k, int64_t *tiles) {
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g <= k; g += gridDim.x * blockDim.x) {
+        int64_t t = 0;
+        if (g < k && cbase[g] >= 0) {
+            const int64_t n = gnm[2 * g];
+            t = ((n + kGramM - 1) / kGramM) * ((n + kGramN - 1) / kGramN);
+        }
+        tiles[g] = t;
+    }
+}
+
+__global__ void __launch_bounds__(kGramThreads, 1) k_dense_gram(GramArgs A) {
+    extern __shared__ uint8_t gram_smem[];
+    __shared__ uint32_t s_taddr;
+    __shared__ __align__(8) uint64_t s_bar[kGramStages];
+    __shared__ long long s_item;
+    using namespace pgd_tc;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    uint8_t *base = gram_smem + ((1024u - (smem_addr(gram_smem) & 1023u)) & 1023u);
+    if (warp == 0) tmem_alloc(&s_taddr, kGramN);
+    if (tid == 0)
+        for (int i = 0; i < kGramStages; i++) mbar_init(&s_bar[i], 1);
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = s_taddr;
+    // read-back role: TMEM lanes 32·(warp & 3), columns 64·(warp >> 2) ...
+    const int lg = warp & 3, cq = warp >> 2;
+    const int64_t total = A.etile[A.k];
+    uint32_t phase = 0, pend = 0;   // thread 0, per stage
+    int chunk = 0;
+    bool bad = false;
+    while (true) {
+        if (tid == 0) s_item = (long long)atomicAdd(A.next, 1ull);
+        __syncthreads();
+        const int64_t item = s_item;
+        __syncthreads();
+        if (item >= total) break;
+        const int g = batch_find(A.etile, A.k, item);
+        const int n = (int)A.gnm[2 * g];
+        const int W = (n + 63) >> 6;
+        const int64_t stride = (int64_t)W * 64;
+        const int tcols = (n + kGramN - 1) / kGramN;
+        const int local = (int)(item - A.etile[g]);
+        const int i0 = (local / tcols) * kGramM, j0 = (local % tcols) * kGramN;
+        const int nt = min(kGramN, ((n - j0 + 15) >> 4) << 4);
+        const uint64_t *rows = A.bits + A.wbase[g];
+        const uint16_t *cng = A.cn + A.cbase[g];
+        const int nK = (n + 15) >> 4;
+        const uint32_t id_pos = idesc_tf32_f32(kGramM, nt, false), id_neg = idesc_tf32_f32(kGramM, nt, true);
+        // this thread's items (4 columns of one row each, 16 bytes): A tile
+        // items 0..511, B tile items after them; in the core-matrix layout
+        // (LBO 128, SBO 512) item i of a tile lives at byte 16·i
+        const int nItems = kGramM * 4 + nt * 4;
+        int grow[3], gblk[3];
+        uint32_t dst[3];
+        bool isA[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const int it = tid + k * kGramThreads;
+            isA[k] = it < kGramM * 4;
+            const int i2 = isA[k] ? it : it - kGramM * 4;
+            const int row = ((i2 >> 5) << 3) | (i2 & 7);
+            const int r = isA[k] ? i0 + row : j0 + row;
+            grow[k] = (it < nItems && r < n) ? r : -1;
+            gblk[k] = (i2 >> 3) & 3;
+            dst[k] = isA[k] ? (uint32_t)(16 * i2) : (uint32_t)(kGramM * 64 + 16 * i2);
+        }
+        for (int ch = 0; ch < 2 * nK; ch++) {
+            const bool second = ch >= nK;   // TA x A, negated
+            const int kc = second ? ch - nK : ch;
+            const int st = chunk % kGramStages;
+            uint8_t *stg = base + st * kGramStageBytes;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                if (tid + k * kGramThreads >= nItems) continue;
+                uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                if (grow[k] >= 0) {
+                    const int k0 = kc * 16 + gblk[k] * 4;   // first column, below 64·W
+                    const uint32_t b4 = (uint32_t)(rows[(int64_t)grow[k] * W + (k0 >> 6)] >> (k0 & 63)) & 15u;
+                    // A x (CN - TA): A side bits, B side CN off the edges;
+                    // TA x A: A side CN on the edges, B side bits
+                    if (isA[k] == second) {
+                        const uint64_t c4 = *(const uint64_t *)(cng + (int64_t)grow[k] * stride + k0);
+                        const uint32_t keep = second ? b4 : ~b4;
+                        v.x = (keep & 1u) ? __float_as_uint((float)(uint32_t)(c4 & 0xffffu)) : 0u;
+                        v.y = (keep & 2u) ? __float_as_uint((float)(uint32_t)((c4 >> 16) & 0xffffu)) : 0u;
+                        v.z = (keep & 4u) ? __float_as_uint((float)(uint32_t)((c4 >> 32) & 0xffffu)) : 0u;
+                        v.w = (keep & 8u) ? __float_as_uint((float)(uint32_t)(c4 >> 48)) : 0u;
+                    } else {
+                        v.x = (b4 & 1u) ? 0x3f800000u : 0u;
+                        v.y = (b4 & 2u) ? 0x3f800000u : 0u;
+                        v.z = (b4 & 4u) ? 0x3f800000u : 0u;
+                        v.w = (b4 & 8u) ? 0x3f800000u : 0u;
+                    }
+                }
+                *(uint4 *)(stg + dst[k]) = v;
+            }
+            fence_async_smem();
+            __syncthreads();   // stage st written
+            if (tid == 0) {
+                fence_after_sync();
+                const uint32_t sa = smem_addr(stg), sb = sa + kGramM * 64;
+#pragma unroll
+                for (int ks = 0; ks < 2; ks++)
+                    mma_tf32(tmem, smem_desc(sa + 256 * ks, 128, 512), smem_desc(sb + 256 * ks, 128, 512),
+                             second ? id_neg : id_pos, (ch | ks) != 0);
+                mma_commit(&s_bar[st]);
+                pend |= 1u << st;
+                // the next chunk's stage must be free: its MMAs (kGramStages - 1 chunks ago) done
+                const int nx = (chunk + 1) % kGramStages;
+                if ((pend >> nx) & 1u) {
+                    bad |= !mbar_wait(&s_bar[nx], (phase >> nx) & 1u, kTcWaitCycles);
+                    phase ^= 1u << nx;
+                    pend &= ~(1u << nx);
+                }
+            }
+            chunk++;
+            if (__syncthreads_or(bad)) {
+                bad = true;
+                break;
+            }
+        }
+        if (bad) break;
+        if (tid == 0)
+            for (int st = 0; st < kGramStages; st++)
+                if ((pend >> st) & 1u) {
+                    bad |= !mbar_wait(&s_bar[st], (phase >> st) & 1u, kTcWaitCycles);
+                    phase ^= 1u << st;
+                    pend &= ~(1u << st);
+                }
+        if (__syncthreads_or(bad)) {
+            bad = true;
+            break;
+        }
+        fence_after_sync();
+        if (cq * 64 < nt) {
+            const int i = i0 + 32 * lg + lane;
+            const int jw = (j0 + cq * 64) >> 6;   // the columns' word of row i
+            uint64_t word = 0;
+            int64_t slot = 0;
+            if (i < n) {
+                const uint64_t *ri = rows + (int64_t)i * W;
+                word = ri[jw];
+                int before = 0;
+                for (int w = 0; w < jw; w++) before += __popcll(ri[w]);
+                slot = A.off[A.vbase[g] + i] + before;
+            }
+            for (int c0 = 0; c0 < 64 && cq * 64 + c0 < nt; c0 += 16) {
+                uint32_t v[16];
+                tmem_ld16(tmem + ((uint32_t)(32 * lg) << 16) + (uint32_t)(cq * 64 + c0), v);
+#pragma unroll
+                for (int e = 0; e < 16; e++)
+                    if ((word >> (c0 + e)) & 1ull) A.eslot[slot++] = (int32_t)__uint_as_float(v[e]);
+            }
+        }
+        fence_before_sync();
+        __syncthreads();   // accumulator read before the next item's MMAs
+    }
+    if (bad && tid == 0) {
+        atomicAdd(A.err, 1ull);
+        for (int st = 0; st < kGramStages; st++)
+            if ((pend >> st) & 1u) mbar_wait(&s_bar[st], (phase >> st) & 1u, kTcWaitCycles);
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, kGramN);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -2016,15 +2248,19 @@ struct DenseView {
     const int64_t *vbase;
     const uint16_t *cn;       // common-neighbour matrices (null: none)
     const int64_t *cbase;     // per graph: first CN entry, or -1
+    int ngraphs;
 };
 
-// k4 of the CN-graph edges whose q has degree in [ctx->tc_min_deg, kTcMaxDeg],
-// on the tensor cores (k_dense_tc): runs of equal q from the sorted dense
-// keys, then one CTA per SM.  *k4_out gets k4 per position of dpos
-// (0xffffffff outside those runs); ctr[8..10] are its run counter, run count
-// and failed-wait count, ctr[11] the counter of k_dense_cn<true>.
+// The tensor-core part of the CN-graph edges: k4 of the runs whose q has
+// degree in [ctx->tc_min_deg, kTcMaxDeg] (k_dense_tc: runs of equal q from
+// the sorted dense keys, one CTA per SM) and E of every CN graph
+// (k_dense_gram).  *k4_out gets k4 per position of dpos (0xffffffff outside
+// those runs), *eslot_out E per adjacency slot.  ctr[8..10]: run counter, run
+// count and failed-wait count; ctr[11]: the counter of k_dense_cn<true>;
+// ctr[12]: the item counter of k_dense_gram.
 static pgd_status dense_tc(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, const DenseView *dense,
-                           const int32_t *dpos, const uint64_t *keys, int64_t ncn, uint32_t **k4_out) {
+                           const int32_t *dpos, const uint64_t *keys, int64_t ncn, uint32_t **k4_out,
+                           int32_t **eslot_out) {
     cudaStream_t s = ctx->stream;
     pgd_status st;
     uint32_t *flag = nullptr, *pos = nullptr, *k4 = nullptr;
@@ -2035,7 +2271,7 @@ static pgd_status dense_tc(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, const 
     if ((st = tg.alloc(&k4, ncn * sizeof(uint32_t)))) return st;
     if ((st = tg.alloc(&runs, (2 * maxruns + 2) * sizeof(int64_t)))) return st;
     unsigned long long *ctr = ctx->d_ctr;
-    PGD_CUDA(ctx, cudaMemsetAsync(ctr + 8, 0, 4 * sizeof(unsigned long long), s));
+    PGD_CUDA(ctx, cudaMemsetAsync(ctr + 8, 0, 5 * sizeof(unsigned long long), s));
     PGD_LAUNCH(ctx, k_tc_run_flags, grid_for(ncn), kThreads, 0, keys, ncn, G.deg, ctx->tc_min_deg, flag);
     PGD_CUDA(ctx, cudaMemsetAsync(flag + ncn, 0, sizeof(uint32_t), s));
     size_t tb = 0;
@@ -2059,7 +2295,36 @@ static pgd_status dense_tc(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, const 
     T.next = ctr + 8;
     T.err = ctr + 10;
     PGD_LAUNCH(ctx, k_dense_tc, ctx->num_sms, kTcThreads, kTcSmem, T);
+    // E of every CN graph: (graph, row tile, column tile) items
+    const int k = dense->ngraphs;
+    int64_t *tiles = nullptr, *etile = nullptr;
+    int32_t *eslot = nullptr;
+    if ((st = tg.alloc(&tiles, ((size_t)k + 1) * sizeof(int64_t)))) return st;
+    if ((st = tg.alloc(&etile, ((size_t)k + 1) * sizeof(int64_t)))) return st;
+    if ((st = tg.alloc(&eslot, ((size_t)2 * G.m + 1) * sizeof(int32_t)))) return st;
+    PGD_LAUNCH(ctx, k_gram_tiles, grid_for(k + 1), kThreads, 0, G.gnm, dense->cbase, k, tiles);
+    tb = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tb, tiles, etile, k + 1, s);
+    if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
+    cub::DeviceScan::ExclusiveSum(tmp, tb, tiles, etile, k + 1, s);
+    pgd_tmp_free(ctx, tmp);
+    PGD_CUDA(ctx, cudaFuncSetAttribute(k_dense_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, kGramSmem));
+    GramArgs E;
+    E.bits = dense->bits;
+    E.wbase = dense->wbase;
+    E.vbase = dense->vbase;
+    E.cn = dense->cn;
+    E.cbase = dense->cbase;
+    E.gnm = G.gnm;
+    E.off = G.off;
+    E.etile = etile;
+    E.k = k;
+    E.eslot = eslot;
+    E.next = ctr + 12;
+    E.err = ctr + 10;
+    PGD_LAUNCH(ctx, k_dense_gram, ctx->num_sms, kGramThreads, kGramSmem, E);
     *k4_out = k4;
+    *eslot_out = eslot;
     return PGD_OK;
 }
 
@@ -2287,8 +2552,9 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
             ncn = (int64_t)h;
         }
         uint32_t *k4pre = nullptr;
+        int32_t *eslot = nullptr;
         if (ncn > 0 && ctx->tc_min_deg > 0) {
-            if ((st = dense_tc(ctx, G, tg, dense, posv + nh, keys2, ncn, &k4pre))) return st;
+            if ((st = dense_tc(ctx, G, tg, dense, posv + nh, keys2, ncn, &k4pre, &eslot))) return st;
             tc_ran = true;
         }
         if (ncn > 0) {
@@ -2301,6 +2567,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
             C.cbase = dense->cbase;
             C.dpos = posv + nh;
             C.k4pre = k4pre;
+            C.eslot = eslot;
             C.ndense = ncn;
             C.next = ctr + 6;
             PGD_LAUNCH(ctx, k_dense_cn<false>, nsm * 8, 256, 0, C);
@@ -2338,7 +2605,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     if (tc_ran) {
         unsigned long long failed = 0;
         PGD_CUDA(ctx, cudaMemcpy(&failed, ctr + 10, sizeof(failed), cudaMemcpyDeviceToHost));
-        if (failed) return pgd_fail(ctx, PGD_ETIMEOUT, "a tensor-core wait in k_dense_tc ran out");
+        if (failed) return pgd_fail(ctx, PGD_ETIMEOUT, "a tensor-core wait in k_dense_tc or k_dense_gram ran out");
     }
     return PGD_OK;
 }
@@ -2603,7 +2870,7 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
     G.egraph = egraph;
     G.gnm = d_gnm;
     G.gdense = ndense_graphs ? d_gdense : nullptr;
-    DenseView dv{(const uint64_t *)bits, d_wbase, d_bases, cn, d_cbase};
+    DenseView dv{(const uint64_t *)bits, d_wbase, d_bases, cn, d_cbase, k};
     StageMs ms;
     BATCH_TRY(run_decompose(ctx, G, (int4 *)U.slot, U.nhubs, U.nhubs_wide, U.max_degree, &ms, ndense_graphs ? &dv : nullptr));
     std::vector<unsigned long long> h((size_t)k * PGD_NSUMS);
@@ -3216,7 +3483,7 @@ pgd_status pgd_dev_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pai
         G.egraph = egraph;
         G.gnm = d_gnm;
         G.gdense = ndense_graphs ? d_gdense : nullptr;
-        DenseView dv{(const uint64_t *)bits, d_wbase, d_vbase, cn, d_cbase};
+        DenseView dv{(const uint64_t *)bits, d_wbase, d_vbase, cn, d_cbase, k};
         PB_TRY(run_decompose(ctx, G, (int4 *)U->slot, U->nhubs, U->nhubs_wide, U->max_degree, &ms, ndense_graphs ? &dv : nullptr));
     }
     std::vector<unsigned long long> h((size_t)k * PGD_NSUMS);

@@ -24,6 +24,13 @@ __device__ __forceinline__ uint32_t idesc_e4m3_f32(int m, int n) {
     return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
+// instruction descriptor of kind::tf32 (format code 2 for A and B), fp32 D, both
+// K-major; negate_a subtracts the product from the accumulator
+__device__ __forceinline__ uint32_t idesc_tf32_f32(int m, int n, bool negate_a) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)negate_a << 13) | ((uint32_t)(n >> 3) << 17) |
+           ((uint32_t)(m >> 4) << 24);
+}
+
 __device__ __forceinline__ void tmem_alloc(uint32_t *dst_smem, uint32_t ncols) {   // one full warp
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst_smem)),
                  "r"(ncols)
@@ -67,6 +74,16 @@ __device__ __forceinline__ void mma_e4m3(uint32_t d_tmem, uint64_t a_desc, uint6
     asm volatile(
         "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
         "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"((uint32_t)accumulate)
+        : "memory");
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, tf32 operands (32-bit containers), fp32 accumulator
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         bool accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
         "l"(a_desc), "l"(b_desc), "r"(idesc), "r"((uint32_t)accumulate)
         : "memory");
 }
