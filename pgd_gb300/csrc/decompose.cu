@@ -1362,8 +1362,7 @@ struct DenseCnArgs {
     const uint16_t *cn;       // CN matrices of the graphs that have one
     const int64_t *cbase;     // per graph: first entry of its CN matrix
     const int32_t *dpos;      // E_ordered positions of those graphs' edges, grouped by q
-    const uint32_t *k4pre;    // per position of dpos: k4 from k_dense_tc, 0xffffffff where not taken (or null)
-    const int32_t *eslot;     // with k4pre: E[x][y] per adjacency slot x -> y, from k_dense_gram
+    const uint32_t *k4pre;    // per position of dpos: 0xffffffff where k_dense_tc did not take the run (or null)
     int64_t ndense;
     unsigned long long *next;
 };
@@ -1371,10 +1370,7 @@ struct DenseCnArgs {
 // Up to kDenseGroup edges (p_j, q) with the same q, as in k_dense; per row
 // word L of A_q the warp reads 64 entries of CN[q] and of each CN[p_j] (two
 // per lane) for the two sums, and the rows of the word's members of T_j.
-// kPre: only the groups whose k4 k_dense_tc counted; their two sums come
-// from E (k_dense_gram) as E[q][p] - d_p, so no row is scanned at all.
-// Otherwise only the other groups.
-template <bool kPre>
+// Groups of the runs k_dense_tc took are left to k_dense_close.
 __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
     __shared__ unsigned long long s_red[8][PGD_NSUMS];
     const DevGraph &G = A.G;
@@ -1401,9 +1397,9 @@ __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
             const int64_t stride = (int64_t)W * 64;
             const uint64_t *rows = A.bits + A.wbase[g];
             const uint16_t *cnb = A.cn + A.cbase[g];
-            // k4 of this group counted on the tensor cores or not (all edges of a
-            // group share q, so all or none are): the other instance takes it
-            if ((A.k4pre && A.k4pre[i0] != 0xffffffffu) != kPre) {
+            // a run taken by the tensor cores (all edges of a group share q, so
+            // all or none of them are) is closed by k_dense_close
+            if (A.k4pre && A.k4pre[i0] != 0xffffffffu) {
                 i0 = i1;
                 continue;
             }
@@ -1431,30 +1427,7 @@ __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
                     pl[j] = (int32_t)p;
                 }
             }
-            unsigned long long dpre[kDenseGroup];   // kPre: E[q][p_j] - d_p (mod 2^64)
-            if constexpr (kPre) {
-                // rank of p_j in N(q): popcounts of A_q's words before p_j's, then of its word below it
-                const int c = __popcll(Aq);
-                int o = c;
-#pragma unroll
-                for (int sft = 1; sft < 32; sft <<= 1) {
-                    const int y = __shfl_up_sync(0xffffffffu, o, sft);
-                    if (lane >= sft) o += y;
-                }
-                o -= c;
-                const int64_t qoff = G.off[qg];
-#pragma unroll
-                for (int j = 0; j < kDenseGroup; j++) {
-                    dpre[j] = 0;
-                    if (j < R) {
-                        const int pw = pl[j] >> 6;
-                        const uint64_t below = __shfl_sync(0xffffffffu, Aq, pw) & ((1ull << (pl[j] & 63)) - 1);
-                        const int rank = __shfl_sync(0xffffffffu, o, pw) + __popcll(below);
-                        dpre[j] = (unsigned long long)(long long)(A.eslot[qoff + rank] - G.deg[vb + pl[j]]);
-                    }
-                }
-            }
-            for (int L = 0; L < W && !kPre; L++) {
+            for (int L = 0; L < W; L++) {
                 // word L of every T_j as 32-bit halves
                 uint32_t tlo[kDenseGroup], thi[kDenseGroup];
                 uint32_t ulo = 0, uhi = 0;
@@ -1513,11 +1486,10 @@ __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
                 if (j >= R) break;
                 const unsigned long long t = pgd_warp_sum(__popcll(T[j]));
                 const unsigned long long nsq = pgd_warp_sum(__popcll(Sq[j]));
-                const unsigned long long k4 = kPre ? A.k4pre[i0 + j] : pgd_warp_sum(k4x2[j]) >> 1;
+                const unsigned long long k4 = pgd_warp_sum(k4x2[j]) >> 1;
                 // sum_{S_q} CN[p][w] - sum_T CN[q][x]: lane shares are signed, the
                 // warp's total modulo 2^64 is exact (|total| < 2^23)
-                const unsigned long long dtot =
-                    kPre ? dpre[j] : pgd_warp_sum((unsigned long long)(long long)dsum[j]);
+                const unsigned long long dtot = pgd_warp_sum((unsigned long long)(long long)dsum[j]);
                 const unsigned long long c = dtot + 2 * k4 + t - nsq;
                 const int64_t e = A.dpos[i0 + j];
                 const int32_t id = G.order[e];
@@ -2067,6 +2039,111 @@ __global__ void __launch_bounds__(kGramThreads, 1) k_dense_gram(GramArgs A) {
     if (warp == 0) tmem_dealloc(tmem, kGramN);
 }
 
+// The edges of the runs k_dense_tc took, one per lane: t = CN[p][q],
+// |S_q| = d_q - t - 1, k4 from k_dense_tc, the two c4 sums from E as
+// E[q][p] - d_p (the slot q -> p: p's rank in N(q) from A_q's popcounts),
+// then the closed forms and the per-edge row.  A warp takes a run at a time.
+struct DenseCloseArgs {
+    DevGraph G;
+    const uint64_t *bits;
+    const int64_t *wbase;
+    const int64_t *vbase;
+    const uint16_t *cn;
+    const int64_t *cbase;
+    const int32_t *dpos;
+    const int64_t *runs;
+    const unsigned long long *nruns;
+    const uint32_t *k4;
+    const int32_t *eslot;
+    unsigned long long *next;
+};
+
+// a warp's per-lane sums of graph g, reduced and added to the graph's sums
+__device__ __forceinline__ void warp_flush_graph(const DevGraph &G, unsigned long long *acc, int g, int lane) {
+#pragma unroll
+    for (int i = 0; i < PGD_NSUMS; i++) {
+        const unsigned long long v = pgd_warp_sum(acc[i]);
+        if (lane == 0 && v) atomicAdd(G.sums + (int64_t)g * PGD_NSUMS + i, v);
+        acc[i] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_dense_close(DenseCloseArgs A) {
+    const DevGraph &G = A.G;
+    const int lane = threadIdx.x & 31;
+    int cur_g = -1;
+    unsigned long long acc[PGD_NSUMS];
+#pragma unroll
+    for (int i = 0; i < PGD_NSUMS; i++) acc[i] = 0;
+    const unsigned long long nruns = *A.nruns;
+    while (true) {
+        unsigned long long r = 0;
+        if (lane == 0) r = atomicAdd(A.next, 1ull);
+        r = __shfl_sync(0xffffffffu, r, 0);
+        if (r >= nruns) break;
+        const int64_t i0 = A.runs[2 * r], i1 = A.runs[2 * r + 1];
+        const int32_t qg = dense_q(G, A.dpos[i0]);
+        const int g = G.egraph[A.dpos[i0]];
+        if (g != cur_g) {
+            if (cur_g >= 0) warp_flush_graph(G, acc, cur_g, lane);
+            cur_g = g;
+        }
+        const int64_t vb = A.vbase[g];
+        const long long n = G.gnm[2 * g], m = G.gnm[2 * g + 1];
+        const int W = (int)((n + 63) >> 6);
+        const int64_t stride = (int64_t)W * 64;
+        const uint64_t *rows = A.bits + A.wbase[g];
+        const uint16_t *cnb = A.cn + A.cbase[g];
+        const int64_t q = qg - vb;
+        const uint64_t Aq = lane < W ? __ldg(rows + q * W + lane) : 0ull;
+        const int c = __popcll(Aq);
+        int o = c;
+#pragma unroll
+        for (int sft = 1; sft < 32; sft <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, o, sft);
+            if (lane >= sft) o += y;
+        }
+        o -= c;
+        const int64_t qoff = G.off[qg];
+        const long long dq = G.deg[qg];
+        for (int64_t b = i0; b < i1; b += 32) {
+            const int64_t i = b + lane;
+            const bool act = i < i1;
+            int64_t e = 0;
+            int32_t v = 0, u = 0, pl = 0;
+            if (act) {
+                e = A.dpos[i];
+                const int32_t id = G.order[e];
+                v = G.ev[id];
+                u = G.eu[id];
+                pl = (int32_t)((v == qg ? u : v) - vb);
+            }
+            const int pw = pl >> 6;
+            const uint64_t aw = __shfl_sync(0xffffffffu, Aq, pw);
+            const int ow = __shfl_sync(0xffffffffu, o, pw);
+            if (act) {
+                const int rank = ow + __popcll(aw & ((1ull << (pl & 63)) - 1));
+                const unsigned long long t = cnb[(int64_t)pl * stride + q];
+                const unsigned long long k4 = A.k4[i];
+                const unsigned long long dsum =
+                    (unsigned long long)(long long)(A.eslot[qoff + rank] - G.deg[vb + pl]);
+                const unsigned long long nsq = (unsigned long long)(dq - (long long)t - 1);
+                const unsigned long long c4 = dsum + 2 * k4 + t - nsq;
+                const long long dv = G.deg[v], du = G.deg[u];
+                pgd_edge_sums(acc, dv, du, t, m, n);
+                acc[3] += k4;
+                acc[4] += c4;
+                if (G.micro) {
+#pragma unroll
+                    for (int col = 0; col < PGD_NMICRO; col++)
+                        G.micro[e * PGD_NMICRO + col] = pgd_micro_col(col, dv, du, t, k4, c4);
+                }
+            }
+        }
+    }
+    if (cur_g >= 0) warp_flush_graph(G, acc, cur_g, lane);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -2254,13 +2331,19 @@ struct DenseView {
 // The tensor-core part of the CN-graph edges: k4 of the runs whose q has
 // degree in [ctx->tc_min_deg, kTcMaxDeg] (k_dense_tc: runs of equal q from
 // the sorted dense keys, one CTA per SM) and E of every CN graph
-// (k_dense_gram).  *k4_out gets k4 per position of dpos (0xffffffff outside
-// those runs), *eslot_out E per adjacency slot.  ctr[8..10]: run counter, run
-// count and failed-wait count; ctr[11]: the counter of k_dense_cn<true>;
+// (k_dense_gram).  out->k4 gets k4 per position of dpos (0xffffffff outside
+// those runs), out->eslot E per adjacency slot, out->runs the runs.  ctr[8..10]: run counter, run
+// count and failed-wait count; ctr[11]: the run counter of k_dense_close;
 // ctr[12]: the item counter of k_dense_gram.
+struct TcOut {
+    uint32_t *k4 = nullptr;
+    int32_t *eslot = nullptr;
+    int64_t *runs = nullptr;
+    const unsigned long long *nruns = nullptr;
+};
+
 static pgd_status dense_tc(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, const DenseView *dense,
-                           const int32_t *dpos, const uint64_t *keys, int64_t ncn, uint32_t **k4_out,
-                           int32_t **eslot_out) {
+                           const int32_t *dpos, const uint64_t *keys, int64_t ncn, TcOut *out) {
     cudaStream_t s = ctx->stream;
     pgd_status st;
     uint32_t *flag = nullptr, *pos = nullptr, *k4 = nullptr;
@@ -2323,8 +2406,10 @@ static pgd_status dense_tc(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, const 
     E.next = ctr + 12;
     E.err = ctr + 10;
     PGD_LAUNCH(ctx, k_dense_gram, ctx->num_sms, kGramThreads, kGramSmem, E);
-    *k4_out = k4;
-    *eslot_out = eslot;
+    out->k4 = k4;
+    out->eslot = eslot;
+    out->runs = runs;
+    out->nruns = ctr + 9;
     return PGD_OK;
 }
 
@@ -2551,10 +2636,9 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
             PGD_CUDA(ctx, cudaStreamSynchronize(s));
             ncn = (int64_t)h;
         }
-        uint32_t *k4pre = nullptr;
-        int32_t *eslot = nullptr;
+        TcOut tc;
         if (ncn > 0 && ctx->tc_min_deg > 0) {
-            if ((st = dense_tc(ctx, G, tg, dense, posv + nh, keys2, ncn, &k4pre, &eslot))) return st;
+            if ((st = dense_tc(ctx, G, tg, dense, posv + nh, keys2, ncn, &tc))) return st;
             tc_ran = true;
         }
         if (ncn > 0) {
@@ -2566,14 +2650,25 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
             C.cn = dense->cn;
             C.cbase = dense->cbase;
             C.dpos = posv + nh;
-            C.k4pre = k4pre;
-            C.eslot = eslot;
+            C.k4pre = tc.k4;
             C.ndense = ncn;
             C.next = ctr + 6;
-            PGD_LAUNCH(ctx, k_dense_cn<false>, nsm * 8, 256, 0, C);
-            if (k4pre) {
-                C.next = ctr + 11;
-                PGD_LAUNCH(ctx, k_dense_cn<true>, nsm * 8, 256, 0, C);
+            PGD_LAUNCH(ctx, k_dense_cn, nsm * 8, 256, 0, C);
+            if (tc.k4) {
+                DenseCloseArgs Z;
+                Z.G = G;
+                Z.bits = dense->bits;
+                Z.wbase = dense->wbase;
+                Z.vbase = dense->vbase;
+                Z.cn = dense->cn;
+                Z.cbase = dense->cbase;
+                Z.dpos = posv + nh;
+                Z.runs = tc.runs;
+                Z.nruns = tc.nruns;
+                Z.k4 = tc.k4;
+                Z.eslot = tc.eslot;
+                Z.next = ctr + 11;
+                PGD_LAUNCH(ctx, k_dense_close, nsm * 8, 256, 0, Z);
             }
         }
         if ((int64_t)nd > ncn) {
