@@ -285,7 +285,7 @@ pgd_status pgd_server_destroy(pgd_server *sv);
  * rows as bitsets (one 2048-bit row per warp), larger ones with sorted
  * lists; those of average degree >= n/16 also get a 16-bit common-neighbour
  * matrix (about 2·n² bytes of device memory while the batch runs).
- * A fourth, tensor_min_degree (0 or 2..1088, default 128): in those
+ * A fourth, tensor_min_degree (0 or 2..1088, default 64): in those
  * common-neighbour graphs, the edges (p, q) whose lower-degree endpoint q has
  * degree in [tensor_min_degree, 1088] get their 4-clique count from a
  * product of q's ego network on the tensor cores (e4m3 0/1 operands, fp32

@@ -1517,15 +1517,19 @@ __global__ void __launch_bounds__(256, 3) k_dense_cn(DenseCnArgs A) {
 // the "compress" of Hacker's Delight §7-4 with its masks computed once per word
 // of A_q), go to shared memory.  Then for each pair of 128-edge tiles and each
 // 256-row tile of N(q), every 64-column chunk is expanded to e4m3 tiles (one B
-// tile shared by both edge tiles) in one of two alternating stages while the
-// tensor cores run the previous chunk's MMAs, which one thread issues into two
-// TMEM accumulators; at the end of a row tile every warp reads back one
+// tile shared by both edge tiles) by 15 builder warps into one of two
+// alternating stages while the tensor cores run the previous chunk's MMAs,
+// which one thread of the last warp issues into two TMEM accumulators.  The
+// builders and the issuing thread meet at per-stage mbarriers only: "full"
+// (every builder warp arrived) and "empty" (tcgen05.commit of the MMAs that
+// read the stage); at the end of a row tile every warp reads back one
 // accumulator quarter (a row per thread) and dots it with the rows' own
 // compact bits.  A one is encoded as 2^-6 (0x08), so that a nibble spreads to
 // four bytes in two instructions; all sums are multiples of 2^-12 below 2^9,
 // exact in fp32.
 
 constexpr int kTcThreads = 512;
+constexpr int kTcBuilders = 15;            // warps that expand operand tiles; the last warp issues the MMAs
 constexpr int kTcM = 128;                  // edges per tile (TMEM lanes); two tiles per pass
 constexpr int kTcN = 256;                  // ego rows per tile (TMEM columns per accumulator)
 constexpr int kTcK = 64;                   // ego columns per stage: one compact word
@@ -1619,8 +1623,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
     __shared__ int16_t s_jrow[2][kTcM];   // compact row of each edge's p in the pass, -1 past the run
     __shared__ float s_part[2][2][kTcM];  // per edge tile and column half
     __shared__ uint32_t s_taddr;
-    __shared__ __align__(8) uint64_t s_bar[2];
+    __shared__ __align__(8) uint64_t s_full[2];
+    __shared__ __align__(8) uint64_t s_empty[2];
     __shared__ long long s_run;
+    __shared__ int s_abort;
     using namespace pgd_tc;
     const DevGraph &G = A.G;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -1629,8 +1635,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
     uint64_t *C = (uint64_t *)(base + 2 * kTcStageBytes);
     if (warp == 0) tmem_alloc(&s_taddr, 2 * kTcN);
     if (tid == 0) {
-        mbar_init(&s_bar[0], 1);
-        mbar_init(&s_bar[1], 1);
+        for (int i = 0; i < 2; i++) {
+            mbar_init(&s_full[i], kTcBuilders);
+            mbar_init(&s_empty[i], 1);
+        }
+        s_abort = 0;
     }
     fence_before_sync();
     __syncthreads();
@@ -1639,8 +1648,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
     // read-back role: edge tile et, column half eh, TMEM lanes 32·(warp & 3)
     const int et = warp >> 3, eh = (warp >> 2) & 1, erow = 32 * (warp & 3) + lane;
     const uint32_t etaddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(et * kTcN);
-    uint32_t phase = 0, pend = 0;   // thread 0, per stage: parity of its next phase, commit outstanding
-    int chunk = 0;
+    const bool issuer = warp == kTcBuilders && lane == 0;
+    int chunk = 0;      // chunks so far: chunk c uses stage c & 1 for the (c >> 1)-th time
+    int last = -1;      // issuer: the last chunk committed
     bool bad = false;
     const int64_t nruns = (int64_t)*A.nruns;
     while (true) {
@@ -1683,23 +1693,34 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
         __syncthreads();
         const int d = s_o[32];   // = deg(q), which the run flags bound; a run beyond the
         if (d > kTcMaxDeg) continue;   // shared-memory limit is left to k_dense_cn
-        const int KW = (d + 63) >> 6;
-        for (int i = tid; i < d * KW; i += kTcThreads) C[i] = 0ull;
+        // compact words per ego row, and the row stride: odd, so that the
+        // rows a warp reads together fall in different banks
+        const int KW = (d + 63) >> 6, KS = KW | 1;
+        for (int i = tid; i < d * KS; i += kTcThreads) C[i] = 0ull;
         __syncthreads();
-        {   // C[j] = compact(A_{col[j]}), lane = word of the uncompacted row
+        {   // C[j] = compact(A_{col[j]}), lane = word of the uncompacted row; four rows in flight
             uint64_t mv[6];
 #pragma unroll
             for (int i = 0; i < 6; i++) mv[i] = s_mv[lane][i];
             const uint64_t mw = s_m[lane];
             const int ow = s_o[lane], cw = __popcll(mw), sh = ow & 63, w0 = ow >> 6;
-            for (int j = warp; j < d; j += kTcThreads / 32) {
-                const int x = s_col[j];
-                if (cw) {
-                    const uint64_t v = tc_compress(__ldg(rows + (int64_t)x * W + lane), mw, mv);
+            constexpr int kWarps = kTcThreads / 32;
+            for (int jb = warp; jb < d; jb += 4 * kWarps) {
+                uint64_t w[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int j = jb + k * kWarps;
+                    w[k] = (cw && j < d) ? __ldg(rows + (int64_t)s_col[j] * W + lane) : 0ull;
+                }
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int j = jb + k * kWarps;
+                    if (!cw || j >= d) continue;
+                    const uint64_t v = tc_compress(w[k], mw, mv);
                     if (v) {
-                        atomicOr((unsigned long long *)&C[j * KW + w0], (unsigned long long)(v << sh));
+                        atomicOr((unsigned long long *)&C[j * KS + w0], (unsigned long long)(v << sh));
                         if (sh && sh + cw > 64)
-                            atomicOr((unsigned long long *)&C[j * KW + w0 + 1], (unsigned long long)(v >> (64 - sh)));
+                            atomicOr((unsigned long long *)&C[j * KS + w0 + 1], (unsigned long long)(v >> (64 - sh)));
                     }
                 }
             }
@@ -1723,71 +1744,70 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
             for (int n0 = 0; n0 < d && !bad; n0 += kTcN) {
                 const int nt = min(kTcN, ((d - n0 + 15) >> 4) << 4);
                 const uint32_t idesc = idesc_e4m3_f32(kTcM, nt);
-                // this thread's items (16 columns of one row each) of every
-                // chunk of this tile: compact source word, shift, destination.
-                // In the core-matrix layout (LBO 128, SBO 512) item i of a tile
-                // lives at byte 16·i; a stage holds A of tile 0, A of tile 1, B.
+                // this builder thread's items (16 columns of one row each) of
+                // every chunk of this tile: compact source word, shift,
+                // destination.  In the core-matrix layout (LBO 128, SBO 512)
+                // item i of a tile lives at byte 16·i; a stage holds A of tile
+                // 0, A of tile 1, B.
                 const int nA = ntiles * kTcM * 4, nItems = nA + nt * 4;
-                int src[4], shf[4];
-                uint32_t dst[4];
+                constexpr int kPer = (2 * kTcM * 4 + kTcN * 4 + 32 * kTcBuilders - 1) / (32 * kTcBuilders);
+                if (warp < kTcBuilders) {
+                    int src[kPer], shf[kPer];
+                    uint32_t dst[kPer];
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    const int it = tid + k * kTcThreads;
-                    const bool isA = it < nA;
-                    const int i2 = isA ? (it & (kTcM * 4 - 1)) : it - nA;
-                    const int row = ((i2 >> 5) << 3) | (i2 & 7);
-                    int cr = -1;
-                    if (it < nItems) cr = isA ? s_jrow[it >> 9][row] : (n0 + row < d ? n0 + row : -1);
-                    src[k] = cr >= 0 ? cr * KW : -1;
-                    shf[k] = 16 * ((i2 >> 3) & 3);
-                    dst[k] = isA ? (uint32_t)((it >> 9) * kTcM * kTcK + 16 * i2) : (uint32_t)(2 * kTcM * kTcK + 16 * i2);
-                }
-                for (int kc = 0; kc < KW; kc++) {
-                    const int st = chunk & 1;
-                    uint8_t *stg = base + st * kTcStageBytes;
-#pragma unroll
-                    for (int k = 0; k < 4; k++) {
-                        if (tid + k * kTcThreads < nItems) {
-                            const uint32_t b16 = src[k] >= 0 ? (uint32_t)(C[src[k] + kc] >> shf[k]) & 0xffffu : 0u;
-                            *(uint4 *)(stg + dst[k]) =
-                                make_uint4(tc_spread4(b16 & 15u), tc_spread4((b16 >> 4) & 15u),
-                                           tc_spread4((b16 >> 8) & 15u), tc_spread4(b16 >> 12));
-                        }
+                    for (int k = 0; k < kPer; k++) {
+                        const int it = tid + k * 32 * kTcBuilders;
+                        const bool isA = it < nA;
+                        const int i2 = isA ? (it & (kTcM * 4 - 1)) : it - nA;
+                        const int row = ((i2 >> 5) << 3) | (i2 & 7);
+                        int cr = -1;
+                        if (it < nItems) cr = isA ? s_jrow[it >> 9][row] : (n0 + row < d ? n0 + row : -1);
+                        src[k] = cr >= 0 ? cr * KS : -1;
+                        shf[k] = 16 * ((i2 >> 3) & 3);
+                        dst[k] = it >= nItems ? 0xffffffffu
+                                 : isA ? (uint32_t)((it >> 9) * kTcM * kTcK + 16 * i2)
+                                       : (uint32_t)(2 * kTcM * kTcK + 16 * i2);
                     }
-                    fence_async_smem();
-                    __syncthreads();   // stage st written
-                    if (tid == 0) {
+                    for (int kc = 0; kc < KW; kc++) {
+                        const int c = chunk + kc, st = c & 1, u = c >> 1;
+                        // the MMAs that read this stage last (chunk c - 2) are done
+                        int ok = 1;
+                        if (lane == 0 && u > 0)
+                            ok = mbar_wait_or_abort(&s_empty[st], (u - 1) & 1, kTcWaitCycles, &s_abort);
+                        bad |= !__shfl_sync(0xffffffffu, ok, 0);
+                        uint8_t *stg = base + st * kTcStageBytes;
+#pragma unroll
+                        for (int k = 0; k < kPer; k++) {
+                            if (dst[k] != 0xffffffffu) {
+                                const uint32_t b16 = src[k] >= 0 ? (uint32_t)(C[src[k] + kc] >> shf[k]) & 0xffffu : 0u;
+                                *(uint4 *)(stg + dst[k]) =
+                                    make_uint4(tc_spread4(b16 & 15u), tc_spread4((b16 >> 4) & 15u),
+                                               tc_spread4((b16 >> 8) & 15u), tc_spread4(b16 >> 12));
+                            }
+                        }
+                        fence_async_smem();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(&s_full[st]);
+                    }
+                } else if (issuer) {
+                    for (int kc = 0; kc < KW; kc++) {
+                        const int c = chunk + kc, st = c & 1, u = c >> 1;
+                        bad |= !mbar_wait_or_abort(&s_full[st], u & 1, kTcWaitCycles, &s_abort);
                         fence_after_sync();
-                        const uint32_t sa = smem_addr(stg), sb = sa + 2 * kTcM * kTcK;
+                        const uint32_t sa = smem_addr(base + st * kTcStageBytes), sb = sa + 2 * kTcM * kTcK;
                         for (int t = 0; t < ntiles; t++)
 #pragma unroll
                             for (int ks = 0; ks < 2; ks++)
-                                mma_e4m3(tmem + (uint32_t)(t * kTcN), smem_desc(sa + t * kTcM * kTcK + 256 * ks, 128, 512),
+                                mma_e4m3(tmem + (uint32_t)(t * kTcN),
+                                         smem_desc(sa + t * kTcM * kTcK + 256 * ks, 128, 512),
                                          smem_desc(sb + 256 * ks, 128, 512), idesc, (kc | ks) != 0);
-                        mma_commit(&s_bar[st]);
-                        pend |= 1u << st;
-                        // the next chunk overwrites the other stage: its MMAs must be done
-                        if ((pend >> (st ^ 1)) & 1u) {
-                            bad |= !mbar_wait(&s_bar[st ^ 1], (phase >> (st ^ 1)) & 1u, kTcWaitCycles);
-                            phase ^= 1u << (st ^ 1);
-                            pend &= ~(1u << (st ^ 1));
-                        }
+                        mma_commit(&s_empty[st]);
+                        last = c;
                     }
-                    chunk++;
-                    if (__syncthreads_or(bad)) {
-                        bad = true;
-                        break;
-                    }
+                    // the accumulators are complete once the last commit lands
+                    bad |= !mbar_wait_or_abort(&s_empty[last & 1], (last >> 1) & 1, kTcWaitCycles, &s_abort);
                 }
-                if (bad) break;
-                // the accumulators are complete once the last commits land
-                if (tid == 0)
-                    for (int st = 0; st < 2; st++)
-                        if ((pend >> st) & 1u) {
-                            bad |= !mbar_wait(&s_bar[st], (phase >> st) & 1u, kTcWaitCycles);
-                            phase ^= 1u << st;
-                            pend &= ~(1u << st);
-                        }
+                chunk += KW;
                 if (__syncthreads_or(bad)) {
                     bad = true;
                     break;
@@ -1801,7 +1821,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
                         tmem_ld16(etaddr + (uint32_t)c0, v);
                         const int y0 = n0 + c0;   // a multiple of 16, below d
                         const uint32_t b16 =
-                            jr >= 0 ? (uint32_t)(C[jr * KW + (y0 >> 6)] >> (y0 & 63)) & 0xffffu : 0u;
+                            jr >= 0 ? (uint32_t)(C[jr * KS + (y0 >> 6)] >> (y0 & 63)) & 0xffffu : 0u;
 #pragma unroll
                         for (int i = 0; i < 16; i++) acc += ((b16 >> i) & 1u) ? __uint_as_float(v[i]) : 0.f;
                     }
@@ -1821,12 +1841,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
         }
         if (bad) break;
     }
-    if (bad) {
-        if (tid == 0) {
-            atomicAdd(A.err, 1ull);
-            for (int st = 0; st < 2; st++)   // MMAs still in flight: one more bounded wait each
-                if ((pend >> st) & 1u) mbar_wait(&s_bar[st], (phase >> st) & 1u, kTcWaitCycles);
-        }
+    if (bad && issuer) {
+        atomicAdd(A.err, 1ull);
+        // MMAs still in flight: one more bounded wait for the last commit
+        if (last >= 0) mbar_wait(&s_empty[last & 1], (last >> 1) & 1, kTcWaitCycles);
     }
     fence_before_sync();
     __syncthreads();

@@ -27,7 +27,7 @@ struct pgd_ctx {
     int anchor_hub = 64;     // anchors of degree >= this take the bitmap (block) path
     int cache_hub = 32;      // W(w,p) taken from the per-anchor histogram for neighbours of degree >= this
     int dense_max = 2048;    // batched graphs with at most this many vertices use row bitsets
-    int tc_min_deg = 128;    // batched CN-graph runs with d_q >= this count k4 on the tensor cores (0: never)
+    int tc_min_deg = 64;     // batched CN-graph runs with d_q >= this count k4 on the tensor cores (0: never)
 };
 
 struct pgd_graph {

@@ -68,6 +68,34 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long l
     }
 }
 
+// as mbar_wait, but returns false at once when *abort is set, and sets it
+// when its own limit runs out (so that the other waiters stop too)
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t *bar, uint32_t parity, long long limit,
+                                                   volatile int *abort) {
+    const uint32_t a = smem_addr(bar);
+    const long long t0 = clock64();
+    while (true) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if (*abort) return false;
+        if (clock64() - t0 > limit) {
+            *abort = 1;
+            return false;
+        }
+    }
+}
+
+// one arrival on the mbarrier (release: this thread's earlier writes are seen
+// by whoever waits for the phase)
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(smem_addr(bar)) : "memory");
+}
+
 // D[tmem] (+)= A[smem] * B[smem]^T, e4m3 operands, fp32 accumulator
 __device__ __forceinline__ void mma_e4m3(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
                                          bool accumulate) {
