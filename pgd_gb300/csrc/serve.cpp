@@ -50,12 +50,13 @@ struct Request {
 // Device bytes one request needs while it is decomposed: pairs and their
 // sort buffers, the CSR with its per-slot arrays, per-edge and per-vertex
 // work arrays, and for graphs of at most 2048 vertices their adjacency
-// bit rows and 16-bit common-neighbour matrix.  Deliberately generous; only
-// used for admission.
+// bit rows, 16-bit common-neighbour matrix and the tensor-core path's
+// per-edge arrays (run flags and positions, k4, E per slot).  Deliberately
+// generous; only used for admission.
 uint64_t estimate_bytes(int64_t pairs, int64_t n) {
     const uint64_t p = (uint64_t)std::max<int64_t>(pairs, 1), v = (uint64_t)std::max<int64_t>(n, 1);
     uint64_t bytes = 160 * p + 64 * v + (64u << 10);
-    if (v <= 2048) bytes += 2 * v * (v + 64) + 8 * v * ((v + 63) / 64);
+    if (v <= 2048) bytes += 2 * v * (v + 64) + 8 * v * ((v + 63) / 64) + 24 * p;
     return bytes;
 }
 
