@@ -1666,6 +1666,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
         const int W = (int)((G.gnm[2 * g] + 63) >> 6);
         const uint64_t *rows = A.bits + A.wbase[g];
         const int64_t q = qg - vb;
+        // the first pass's edges: their other endpoints p, loaded now so that
+        // the latency of the chain hides under the compaction
+        int pfirst = 0;
+        if (tid < 2 * kTcM && tid < (int)(i1 - i0)) {
+            const int32_t id = G.order[A.dpos[i0 + tid]];
+            const int32_t v = G.ev[id], u = G.eu[id];
+            pfirst = (int)((v == qg ? u : v) - vb);
+        }
         if (warp == 0) {
             const uint64_t mq = lane < W ? __ldg(rows + q * W + lane) : 0ull;
             const int c = __popcll(mq);
@@ -1683,12 +1691,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
             tc_compress_masks(mq, mv);
 #pragma unroll
             for (int i = 0; i < 6; i++) s_mv[lane][i] = mv[i];
-            uint64_t b = mq;
-            for (int j = o; b; j++) {
-                const int t = __ffsll(b) - 1;
-                b &= b - 1;
-                if (j < kTcMaxDeg) s_col[j] = (uint16_t)(64 * lane + t);
-            }
         }
         __syncthreads();
         const int d = s_o[32];   // = deg(q), which the run flags bound; a run beyond the
@@ -1696,32 +1698,61 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
         // compact words per ego row, and the row stride: odd, so that the
         // rows a warp reads together fall in different banks
         const int KW = (d + 63) >> 6, KS = KW | 1;
+        // N(q) in ascending order (four bits of A_q per thread) and the compact rows cleared
+        for (int t = tid; t < 32 * 16; t += kTcThreads) {
+            const int w = t >> 4, b0 = 4 * (t & 15);
+            const uint64_t mw = s_m[w];
+            uint32_t nib = (uint32_t)(mw >> b0) & 15u;
+            int j = s_o[w] + __popcll(mw & ((1ull << b0) - 1));
+            while (nib) {
+                s_col[j++] = (uint16_t)(64 * w + b0 + __ffs(nib) - 1);
+                nib &= nib - 1;
+            }
+        }
         for (int i = tid; i < d * KS; i += kTcThreads) C[i] = 0ull;
         __syncthreads();
-        {   // C[j] = compact(A_{col[j]}), lane = word of the uncompacted row; four rows in flight
+        {   // C[j] = compact(A_{col[j]}), lane = word of the uncompacted row; eight rows in
+            // flight.  Lane w's compressed bits start at bit ow of the compact row, in word
+            // w0; the lanes starting in one word form a contiguous segment, and only the
+            // segment's last lane can spill into the next word.  A segmented OR-scan over
+            // the lanes assembles each word in its segment's last lane: no atomics.
             uint64_t mv[6];
 #pragma unroll
             for (int i = 0; i < 6; i++) mv[i] = s_mv[lane][i];
             const uint64_t mw = s_m[lane];
             const int ow = s_o[lane], cw = __popcll(mw), sh = ow & 63, w0 = ow >> 6;
-            constexpr int kWarps = kTcThreads / 32;
-            for (int jb = warp; jb < d; jb += 4 * kWarps) {
-                uint64_t w[4];
+            const bool spills = sh && sh + cw > 64;
+            const int w0prev = __shfl_up_sync(0xffffffffu, w0, 1), w0next = __shfl_down_sync(0xffffffffu, w0, 1);
+            const bool first = lane == 0 || w0prev != w0, lastl = lane == 31 || w0next != w0;
+            unsigned same = 0;   // bit i: lane - 2^i is in this lane's segment
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
+            for (int i = 0; i < 5; i++) {
+                const int o2 = __shfl_up_sync(0xffffffffu, w0, 1 << i);
+                if (lane >= (1 << i) && o2 == w0) same |= 1u << i;
+            }
+            constexpr int kWarps = kTcThreads / 32, kFly = 8;
+            for (int jb = warp; jb < d; jb += kFly * kWarps) {
+                uint64_t w[kFly];
+#pragma unroll
+                for (int k = 0; k < kFly; k++) {
                     const int j = jb + k * kWarps;
                     w[k] = (cw && j < d) ? __ldg(rows + (int64_t)s_col[j] * W + lane) : 0ull;
                 }
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    const int j = jb + k * kWarps;
-                    if (!cw || j >= d) continue;
-                    const uint64_t v = tc_compress(w[k], mw, mv);
-                    if (v) {
-                        atomicOr((unsigned long long *)&C[j * KS + w0], (unsigned long long)(v << sh));
-                        if (sh && sh + cw > 64)
-                            atomicOr((unsigned long long *)&C[j * KS + w0 + 1], (unsigned long long)(v >> (64 - sh)));
+                for (int k = 0; k < kFly; k++) {
+                    const int j = jb + k * kWarps;   // uniform over the warp
+                    if (j >= d) break;
+                    const uint64_t v = cw ? tc_compress(w[k], mw, mv) : 0ull;
+                    const uint64_t hi = spills ? v >> (64 - sh) : 0ull;
+                    const uint64_t hprev = __shfl_up_sync(0xffffffffu, hi, 1);
+                    uint64_t val = (v << sh) | (first && lane > 0 ? hprev : 0ull);
+#pragma unroll
+                    for (int i = 0; i < 5; i++) {
+                        const uint64_t t = __shfl_up_sync(0xffffffffu, val, 1 << i);
+                        if ((same >> i) & 1u) val |= t;
                     }
+                    if (lastl && w0 < KW) C[j * KS + w0] = val;
+                    if (lane == 31 && hi) C[j * KS + w0 + 1] = hi;
                 }
             }
         }
@@ -1732,9 +1763,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
             if (tid < 2 * kTcM) {
                 int jr = -1;
                 if (m0 + tid < rr) {
-                    const int32_t id = G.order[A.dpos[i0 + m0 + tid]];
-                    const int32_t v = G.ev[id], u = G.eu[id];
-                    const int p = (int)((v == qg ? u : v) - vb);
+                    int p = pfirst;
+                    if (m0 > 0) {
+                        const int32_t id = G.order[A.dpos[i0 + m0 + tid]];
+                        const int32_t v = G.ev[id], u = G.eu[id];
+                        p = (int)((v == qg ? u : v) - vb);
+                    }
                     jr = s_o[p >> 6] + __popcll(s_m[p >> 6] & ((1ull << (p & 63)) - 1));
                 }
                 s_jrow[tid >> 7][tid & (kTcM - 1)] = (int16_t)jr;
