@@ -1786,7 +1786,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
                 const int nA = ntiles * kTcM * 4, nItems = nA + nt * 4;
                 constexpr int kPer = (2 * kTcM * 4 + kTcN * 4 + 32 * kTcBuilders - 1) / (32 * kTcBuilders);
                 if (warp < kTcBuilders) {
-                    int src[kPer], shf[kPer];
+                    // per item: its 16 bits of chunk 0 as a halfword of C (chunk kc
+                    // is 4·kc halfwords further), and its destination.  Rows past
+                    // the run's edges and past d_q are not built: they only feed
+                    // accumulator rows and columns that are never read (stale
+                    // stage bytes there are harmless: the read-back selects by the
+                    // row's bits, which are zero past d_q).
+                    const uint16_t *C16 = (const uint16_t *)C;
+                    int src[kPer];
                     uint32_t dst[kPer];
 #pragma unroll
                     for (int k = 0; k < kPer; k++) {
@@ -1796,9 +1803,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
                         const int row = ((i2 >> 5) << 3) | (i2 & 7);
                         int cr = -1;
                         if (it < nItems) cr = isA ? s_jrow[it >> 9][row] : (n0 + row < d ? n0 + row : -1);
-                        src[k] = cr >= 0 ? cr * KS : -1;
-                        shf[k] = 16 * ((i2 >> 3) & 3);
-                        dst[k] = it >= nItems ? 0xffffffffu
+                        src[k] = 4 * cr * KS + ((i2 >> 3) & 3);
+                        dst[k] = cr < 0 ? 0xffffffffu
                                  : isA ? (uint32_t)((it >> 9) * kTcM * kTcK + 16 * i2)
                                        : (uint32_t)(2 * kTcM * kTcK + 16 * i2);
                     }
@@ -1810,14 +1816,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
                             ok = mbar_wait_or_abort(&s_empty[st], (u - 1) & 1, kTcWaitCycles, &s_abort);
                         bad |= !__shfl_sync(0xffffffffu, ok, 0);
                         uint8_t *stg = base + st * kTcStageBytes;
+                        uint32_t b16[kPer];
+#pragma unroll
+                        for (int k = 0; k < kPer; k++) b16[k] = dst[k] != 0xffffffffu ? C16[src[k] + 4 * kc] : 0u;
 #pragma unroll
                         for (int k = 0; k < kPer; k++) {
-                            if (dst[k] != 0xffffffffu) {
-                                const uint32_t b16 = src[k] >= 0 ? (uint32_t)(C[src[k] + kc] >> shf[k]) & 0xffffu : 0u;
+                            if (dst[k] != 0xffffffffu)
                                 *(uint4 *)(stg + dst[k]) =
-                                    make_uint4(tc_spread4(b16 & 15u), tc_spread4((b16 >> 4) & 15u),
-                                               tc_spread4((b16 >> 8) & 15u), tc_spread4(b16 >> 12));
-                            }
+                                    make_uint4(tc_spread4(b16[k] & 15u), tc_spread4((b16[k] >> 4) & 15u),
+                                               tc_spread4((b16[k] >> 8) & 15u), tc_spread4(b16[k] >> 12));
                         }
                         fence_async_smem();
                         __syncwarp();
