@@ -1666,11 +1666,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
         const int W = (int)((G.gnm[2 * g] + 63) >> 6);
         const uint64_t *rows = A.bits + A.wbase[g];
         const int64_t q = qg - vb;
-        // the first pass's edges: their other endpoints p, loaded now so that
-        // the latency of the chain hides under the compaction
+        // the first pass's edges: their other endpoints p, loaded by the upper
+        // half of the CTA now, so that the latency of the chain hides under the
+        // set-up (warp 0) and the compaction
+        const int ptid = tid - (kTcThreads - 2 * kTcM);   // this thread's edge of the first pass, if >= 0
         int pfirst = 0;
-        if (tid < 2 * kTcM && tid < (int)(i1 - i0)) {
-            const int32_t id = G.order[A.dpos[i0 + tid]];
+        if (ptid >= 0 && ptid < (int)(i1 - i0)) {
+            const int32_t id = G.order[A.dpos[i0 + ptid]];
             const int32_t v = G.ev[id], u = G.eu[id];
             pfirst = (int)((v == qg ? u : v) - vb);
         }
@@ -1760,18 +1762,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
         for (int m0 = 0; m0 < rr && !bad; m0 += 2 * kTcM) {
             const int ntiles = rr - m0 > kTcM ? 2 : 1;   // edge tiles of this pass
             __syncthreads();   // C complete; the previous pass's s_jrow and s_part read
-            if (tid < 2 * kTcM) {
+            if (ptid >= 0) {
                 int jr = -1;
-                if (m0 + tid < rr) {
+                if (m0 + ptid < rr) {
                     int p = pfirst;
                     if (m0 > 0) {
-                        const int32_t id = G.order[A.dpos[i0 + m0 + tid]];
+                        const int32_t id = G.order[A.dpos[i0 + m0 + ptid]];
                         const int32_t v = G.ev[id], u = G.eu[id];
                         p = (int)((v == qg ? u : v) - vb);
                     }
                     jr = s_o[p >> 6] + __popcll(s_m[p >> 6] & ((1ull << (p & 63)) - 1));
                 }
-                s_jrow[tid >> 7][tid & (kTcM - 1)] = (int16_t)jr;
+                s_jrow[ptid >> 7][ptid & (kTcM - 1)] = (int16_t)jr;
             }
             __syncthreads();
             float acc = 0.f;   // row erow of edge tile et, column half eh
@@ -1857,14 +1859,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_dense_tc(DenseTcArgs A) {
                 if (et < ntiles) {
                     const int jr = s_jrow[et][erow];
                     const int cend = min(nt, eh * 128 + 128);
-                    for (int c0 = eh * 128; c0 < cend; c0 += 16) {
-                        uint32_t v[16];
-                        tmem_ld16(etaddr + (uint32_t)c0, v);
-                        const int y0 = n0 + c0;   // a multiple of 16, below d
-                        const uint32_t b16 =
-                            jr >= 0 ? (uint32_t)(C[jr * KS + (y0 >> 6)] >> (y0 & 63)) & 0xffffu : 0u;
+                    // 32 columns per step: two loads in flight, one wait
+                    for (int c0 = eh * 128; c0 < cend; c0 += 32) {
+                        uint32_t v[32];
+                        const bool two = c0 + 16 < cend;   // nt is a multiple of 16
+                        tmem_ld16_async(etaddr + (uint32_t)c0, v);
+                        if (two) tmem_ld16_async(etaddr + (uint32_t)(c0 + 16), v + 16);
+                        const int y0 = n0 + c0;   // a multiple of 32, below d
+                        const uint32_t b32 = jr >= 0 ? (uint32_t)(C[jr * KS + (y0 >> 6)] >> (y0 & 63)) : 0u;
+                        tmem_wait_ld();
 #pragma unroll
-                        for (int i = 0; i < 16; i++) acc += ((b16 >> i) & 1u) ? __uint_as_float(v[i]) : 0.f;
+                        for (int i = 0; i < 16; i++) acc += ((b32 >> i) & 1u) ? __uint_as_float(v[i]) : 0.f;
+                        if (two) {
+#pragma unroll
+                            for (int i = 16; i < 32; i++) acc += ((b32 >> i) & 1u) ? __uint_as_float(v[i]) : 0.f;
+                        }
                     }
                 }
                 fence_before_sync();
