@@ -2006,22 +2006,41 @@ __global__ void __launch_bounds__(kGramThreads, 1) k_dense_gram(GramArgs A) {
             gblk[k] = (i2 >> 3) & 3;
             dst[k] = isA[k] ? (uint32_t)(16 * i2) : (uint32_t)(kGramM * 64 + 16 * i2);
         }
+        // the global words of one chunk's items: the bit-row word and, where the
+        // item takes CN, its four entries; loaded one chunk ahead
+        auto fetch = [&](int ch, uint64_t *bw, uint64_t *cw) {
+            const bool second = ch >= nK;
+            const int kc = second ? ch - nK : ch;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                bw[k] = cw[k] = 0ull;
+                if (tid + k * kGramThreads < nItems && grow[k] >= 0) {
+                    const int k0 = kc * 16 + gblk[k] * 4;   // first column, below 64·W
+                    bw[k] = rows[(int64_t)grow[k] * W + (k0 >> 6)];
+                    if (isA[k] == second) cw[k] = *(const uint64_t *)(cng + (int64_t)grow[k] * stride + k0);
+                }
+            }
+        };
+        uint64_t pbw[3], pcw[3];
+        fetch(0, pbw, pcw);
         for (int ch = 0; ch < 2 * nK; ch++) {
             const bool second = ch >= nK;   // TA x A, negated
             const int kc = second ? ch - nK : ch;
             const int st = chunk % kGramStages;
             uint8_t *stg = base + st * kGramStageBytes;
+            uint64_t nbw[3] = {0ull, 0ull, 0ull}, ncw[3] = {0ull, 0ull, 0ull};
+            if (ch + 1 < 2 * nK) fetch(ch + 1, nbw, ncw);
 #pragma unroll
             for (int k = 0; k < 3; k++) {
                 if (tid + k * kGramThreads >= nItems) continue;
                 uint4 v = make_uint4(0u, 0u, 0u, 0u);
                 if (grow[k] >= 0) {
-                    const int k0 = kc * 16 + gblk[k] * 4;   // first column, below 64·W
-                    const uint32_t b4 = (uint32_t)(rows[(int64_t)grow[k] * W + (k0 >> 6)] >> (k0 & 63)) & 15u;
+                    const int k0 = kc * 16 + gblk[k] * 4;
+                    const uint32_t b4 = (uint32_t)(pbw[k] >> (k0 & 63)) & 15u;
                     // A x (CN - TA): A side bits, B side CN off the edges;
                     // TA x A: A side CN on the edges, B side bits
                     if (isA[k] == second) {
-                        const uint64_t c4 = *(const uint64_t *)(cng + (int64_t)grow[k] * stride + k0);
+                        const uint64_t c4 = pcw[k];
                         const uint32_t keep = second ? b4 : ~b4;
                         v.x = (keep & 1u) ? __float_as_uint((float)(uint32_t)(c4 & 0xffffu)) : 0u;
                         v.y = (keep & 2u) ? __float_as_uint((float)(uint32_t)((c4 >> 16) & 0xffffu)) : 0u;
@@ -2035,6 +2054,11 @@ __global__ void __launch_bounds__(kGramThreads, 1) k_dense_gram(GramArgs A) {
                     }
                 }
                 *(uint4 *)(stg + dst[k]) = v;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                pbw[k] = nbw[k];
+                pcw[k] = ncw[k];
             }
             fence_async_smem();
             __syncthreads();   // stage st written
