@@ -316,8 +316,8 @@ pgd_status pgd_autotune(pgd_ctx *ctx, pgd_graph *const *graphs, int k, int reps,
  * static device array of pgd_noalloc_scratch_bytes() bytes (64 MiB) that the
  * library reserves on every GPU it is loaded on; the call never allocates.
  * Graphs that need more scratch than that are refused with PGD_ENOMEM and a
- * message in err.  The first call on a device looks up the array's address,
- * so make it before any stream capture.  All calls share the array and each
+ * message in err.  The first call on a device looks up the array's address.
+ * All calls share the array and each
  * clears what must start at zero: calls that overlap on the GPU race and must
  * be serialised by the caller.  The call synchronises `stream` up to four
  * times, because later launch sizes (hub-anchored edges, work items) are read

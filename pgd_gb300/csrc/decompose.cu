@@ -3096,9 +3096,8 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
 //
 // Some callers cannot allocate device memory at the moment they need counts:
 // code inside a framework that hands out a fixed workspace and forbids
-// allocation (inference plugins, custom ops), code recorded into a CUDA
-// stream capture where cudaMalloc is not permitted, and latency-critical
-// loops where cudaMalloc/cudaFree would synchronise the device.  For them
+// allocation (inference plugins, custom ops), and latency-critical loops
+// where cudaMalloc/cudaFree would synchronise the device.  For them
 // pgd_decompose_csr_noalloc runs the same kernels on a caller's device CSR
 // with every intermediate carved out of one file-scope device array of
 // kNoAllocScratchBytes, and it never calls cudaMalloc, cudaFree or an
@@ -3110,8 +3109,7 @@ pgd_status pgd_dev_decompose_batch(pgd_ctx *ctx, pgd_graph *const *graphs, int k
 // GPU (two streams, two threads) race on it and must be serialised by the
 // caller.  Host code must not use the array's name as an address: its
 // device address is looked up with cudaGetSymbolAddress once per device, by
-// the first call on that device, so that first call should come before any
-// stream capture.
+// the first call on that device.
 
 namespace {
 
