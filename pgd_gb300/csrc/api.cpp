@@ -386,10 +386,33 @@ extern "C" pgd_status pgd_get_edges(pgd_graph *g, int64_t *ev, int64_t *eu, int3
     return PGD_OK;
 }
 
+// The device's address of host memory it can access directly (page-locked
+// and mapped, e.g. from cudaHostAlloc or cudaHostRegister), else null.
+void *pgd_device_view(const void *host) {
+    if (!host) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 extern "C" pgd_status pgd_get_micro(pgd_graph *g, int64_t *src1, int64_t *dst1, uint64_t *cols) {
     if (!g) return PGD_EINVAL;
     if (!g->has_micro) return pgd_fail(g->ctx, PGD_EINVAL, "no per-edge results: decompose with PGD_MICRO first");
     cudaSetDevice(g->ctx->device);
+    // page-locked destinations: one kernel writes rows and ids through the
+    // mapping (every SM's bandwidth over the host link; one copy engine here
+    // moves about 20 GB/s)
+    void *vc = pgd_device_view(cols), *vs = pgd_device_view(src1), *vd = pgd_device_view(dst1);
+    const bool aligned = ((uintptr_t)vc & 15) == 0 && ((uintptr_t)vs & 7) == 0 && ((uintptr_t)vd & 7) == 0;
+    if (aligned && (!cols || vc) && (!src1 || vs) && (!dst1 || vd)) {
+        pgd_status st = pgd_dev_micro_out(g, (uint64_t *)vc, (int64_t *)vs, (int64_t *)vd);
+        if (st) return st;
+        PGD_CUDA(g->ctx, cudaStreamSynchronize(g->ctx->stream));
+        return PGD_OK;
+    }
     if (cols && g->norder)
         PGD_CUDA(g->ctx, pgd_copy_sync(g->ctx, cols, g->micro, g->norder * PGD_NMICRO * sizeof(uint64_t),
                                        cudaMemcpyDeviceToHost));

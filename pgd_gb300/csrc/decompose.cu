@@ -297,13 +297,14 @@ __global__ void k_tslot(DevGraph G, int4 *slot, const int32_t *pos, int64_t coun
 // work plan: hub-anchored edges grouped by anchor, light edges listed
 
 // Sort keys of the work plan, with the E_ordered position as the value.
-// Hub-anchored edges: (rank(anchor) << 32 | position), so one sort groups
+// Hub-anchored edges: (rank(anchor) << eb | position), so one sort groups
 // them by anchor, highest-degree anchors first (the largest work items are
 // handed out first).  (Heaviest-edge-first within an anchor shortens the
 // items' tails but was measured slower: all warps then gather hub lists at
-// once.)  The rest: (~0 << 32 | position), dense-graph edges (batches only)
-// 0xfffffffe, so the sorted order is [hub-anchored, by anchor][dense][light].
-__global__ void k_plan_keys(DevGraph G, uint64_t *keys, int32_t *vals, unsigned long long *counts) {
+// once.)  Dense-graph edges (batches only) get class n, the rest n + 1, so
+// the sorted order is [hub-anchored, by anchor][dense][light].  eb bits hold
+// a position; the sort needs eb + bits(n + 2) key bits.
+__global__ void k_plan_keys(DevGraph G, uint64_t *keys, int32_t *vals, unsigned long long *counts, int eb) {
     unsigned long long hubs = 0, dense = 0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < G.npos; e += (int64_t)gridDim.x * blockDim.x) {
         const int32_t id = G.order[e];
@@ -311,8 +312,8 @@ __global__ void k_plan_keys(DevGraph G, uint64_t *keys, int32_t *vals, unsigned 
         const int32_t p = ranks_above(v, u, G.deg) ? v : u;
         const bool d = dense_edge(G, e);
         const bool hub = !d && G.deg[p] >= G.anchor_hub;
-        const uint32_t hi = d ? 0xfffffffeu : (hub ? (uint32_t)G.vrank[p] : 0xffffffffu);
-        keys[e] = ((uint64_t)hi << 32) | (uint32_t)e;
+        const uint64_t cls = d ? (uint64_t)G.n : (hub ? (uint64_t)G.vrank[p] : (uint64_t)G.n + 1);
+        keys[e] = (cls << eb) | (uint64_t)e;
         vals[e] = (int32_t)e;
         hubs += hub;
         dense += d;
@@ -327,20 +328,20 @@ __global__ void k_plan_keys(DevGraph G, uint64_t *keys, int32_t *vals, unsigned 
 
 // item i starts a chunk: the first edge of an anchor's run of L edges, or
 // every c-th of it, c = ceil(L / min(ceil(L / kChunk), kMaxChunks))
-__global__ void k_item_flags(const uint64_t *keys, int64_t nh, uint32_t *flag) {
+__global__ void k_item_flags(const uint64_t *keys, int64_t nh, uint32_t *flag, int eb) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nh; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t p = (uint32_t)(keys[i] >> 32);
+        const uint64_t p = keys[i] >> eb;
         // first index of this anchor's run
         int64_t lo = 0, hi = i;
         while (lo < hi) {
             int64_t mid = (lo + hi) >> 1;
-            if ((uint32_t)(keys[mid] >> 32) < p) lo = mid + 1; else hi = mid;
+            if ((keys[mid] >> eb) < p) lo = mid + 1; else hi = mid;
         }
         // one past its last index
         int64_t lo2 = i + 1, hi2 = nh;
         while (lo2 < hi2) {
             int64_t mid = (lo2 + hi2) >> 1;
-            if ((uint32_t)(keys[mid] >> 32) <= p) lo2 = mid + 1; else hi2 = mid;
+            if ((keys[mid] >> eb) <= p) lo2 = mid + 1; else hi2 = mid;
         }
         const int64_t L = lo2 - lo;
         const int64_t chunks = min((L + kChunk - 1) / kChunk, (int64_t)kMaxChunks);
@@ -1188,16 +1189,17 @@ __device__ __forceinline__ int32_t dense_q(const DevGraph &G, int64_t e) {
 }
 
 // Sort keys grouping the dense-graph edges by q (then by position), so that
-// k_dense can serve several edges with one pass over A_q's rows.  Edges of
-// graphs with a common-neighbour matrix (cbase[g] >= 0) sort first: bit 63
-// is free because q < 2^31.
+// k_dense can serve several edges with one pass over A_q's rows:
+// (plain << (qb + eb)) | (q << eb) | position, q below 2^qb and positions
+// below 2^eb.  Edges of graphs with a common-neighbour matrix (cbase[g] >= 0,
+// plain = 0) sort first.
 __global__ void k_dense_keys(DevGraph G, const int32_t *dpos, int64_t nd, const int64_t *cbase, uint64_t *keys,
-                             int32_t *vals, unsigned long long *ncn) {
+                             int32_t *vals, unsigned long long *ncn, int qb, int eb) {
     unsigned long long cnt = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t e = dpos[i];
         const uint64_t plain = (cbase && cbase[G.egraph[e]] >= 0) ? 0ull : 1ull;
-        keys[i] = (plain << 63) | ((uint64_t)(uint32_t)dense_q(G, e) << 32) | (uint32_t)e;
+        keys[i] = (plain << (qb + eb)) | ((uint64_t)(uint32_t)dense_q(G, e) << eb) | (uint32_t)e;
         vals[i] = e;
         cnt += 1ull - plain;
     }
@@ -1554,26 +1556,27 @@ struct DenseTcArgs {
     unsigned long long *err;            // waits that ran out
 };
 
-// run starts of the CN-graph edges (keys sorted: q in bits 32-62) whose q has
-// degree in [min_deg, kTcMaxDeg]
-__global__ void k_tc_run_flags(const uint64_t *keys, int64_t ncn, const int32_t *deg, int min_deg, uint32_t *flag) {
+// run starts of the CN-graph edges (sorted dense keys: q above the eb
+// position bits) whose q has degree in [min_deg, kTcMaxDeg]
+__global__ void k_tc_run_flags(const uint64_t *keys, int64_t ncn, const int32_t *deg, int min_deg, uint32_t *flag,
+                               int eb) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ncn; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t q = (uint32_t)(keys[i] >> 32) & 0x7fffffffu;
-        const bool start = i == 0 || ((uint32_t)(keys[i - 1] >> 32) & 0x7fffffffu) != q;
+        const uint32_t q = (uint32_t)(keys[i] >> eb);
+        const bool start = i == 0 || (uint32_t)(keys[i - 1] >> eb) != q;
         const int d = deg[q];
         flag[i] = (start && d >= min_deg && d <= kTcMaxDeg) ? 1u : 0u;
     }
 }
 
 __global__ void k_tc_run_fill(const uint64_t *keys, const uint32_t *flag, const uint32_t *pos, int64_t ncn,
-                              int64_t *runs, unsigned long long *nruns) {
+                              int64_t *runs, unsigned long long *nruns, int eb) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ncn; i += (int64_t)gridDim.x * blockDim.x) {
         if (!flag[i]) continue;
-        const uint32_t q = (uint32_t)(keys[i] >> 32) & 0x7fffffffu;
+        const uint32_t q = (uint32_t)(keys[i] >> eb);
         int64_t lo = i + 1, hi = ncn;   // one past the run's last position
         while (lo < hi) {
             const int64_t mid = (lo + hi) >> 1;
-            if (((uint32_t)(keys[mid] >> 32) & 0x7fffffffu) == q) lo = mid + 1; else hi = mid;
+            if ((uint32_t)(keys[mid] >> eb) == q) lo = mid + 1; else hi = mid;
         }
         runs[2 * pos[i]] = i;
         runs[2 * pos[i] + 1] = lo;
@@ -2435,7 +2438,7 @@ struct TcOut {
 };
 
 static pgd_status dense_tc(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, const DenseView *dense,
-                           const int32_t *dpos, const uint64_t *keys, int64_t ncn, TcOut *out) {
+                           const int32_t *dpos, const uint64_t *keys, int64_t ncn, int eb, TcOut *out) {
     cudaStream_t s = ctx->stream;
     pgd_status st;
     uint32_t *flag = nullptr, *pos = nullptr, *k4 = nullptr;
@@ -2447,7 +2450,7 @@ static pgd_status dense_tc(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, const 
     if ((st = tg.alloc(&runs, (2 * maxruns + 2) * sizeof(int64_t)))) return st;
     unsigned long long *ctr = ctx->d_ctr;
     PGD_CUDA(ctx, cudaMemsetAsync(ctr + 8, 0, 5 * sizeof(unsigned long long), s));
-    PGD_LAUNCH(ctx, k_tc_run_flags, grid_for(ncn), kThreads, 0, keys, ncn, G.deg, ctx->tc_min_deg, flag);
+    PGD_LAUNCH(ctx, k_tc_run_flags, grid_for(ncn), kThreads, 0, keys, ncn, G.deg, ctx->tc_min_deg, flag, eb);
     PGD_CUDA(ctx, cudaMemsetAsync(flag + ncn, 0, sizeof(uint32_t), s));
     size_t tb = 0;
     void *tmp = nullptr;
@@ -2455,7 +2458,7 @@ static pgd_status dense_tc(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, const 
     if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
     cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, ncn + 1, s);
     pgd_tmp_free(ctx, tmp);
-    PGD_LAUNCH(ctx, k_tc_run_fill, grid_for(ncn), kThreads, 0, keys, flag, pos, ncn, runs, ctr + 9);
+    PGD_LAUNCH(ctx, k_tc_run_fill, grid_for(ncn), kThreads, 0, keys, flag, pos, ncn, runs, ctr + 9, eb);
     PGD_CUDA(ctx, cudaMemsetAsync(k4, 0xff, ncn * sizeof(uint32_t), s));
     PGD_CUDA(ctx, cudaFuncSetAttribute(k_dense_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
     DenseTcArgs T;
@@ -2543,6 +2546,13 @@ struct Plan {
     int2 *hrec = nullptr;
 };
 
+// bits that hold every value below x (at least one)
+static int bits_for(int64_t x) {
+    int b = 1;
+    while (b < 63 && (int64_t(1) << b) < x) b++;
+    return b;
+}
+
 static pgd_status build_plan(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, Plan *P, uint64_t **keys_out = nullptr,
                              int32_t **vals_out = nullptr, uint64_t **keys2_out = nullptr) {
     cudaStream_t s = ctx->stream;
@@ -2559,24 +2569,30 @@ static pgd_status build_plan(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, Plan
     // [5] triangle-pass item counter
     unsigned long long *ctr = ctx->d_ctr;
     PGD_CUDA(ctx, cudaMemsetAsync(ctr, 0, 8 * sizeof(unsigned long long), s));
-    PGD_LAUNCH(ctx, k_plan_keys, grid_for(m), kThreads, 0, G, keys, vals, ctr);
-    size_t tb = 0;
-    void *tmp = nullptr;
-    cub::DeviceRadixSort::SortPairs(nullptr, tb, keys, keys2, vals, P->posv, m, 0, 64, s);
-    if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
-    cub::DeviceRadixSort::SortPairs(tmp, tb, keys, keys2, vals, P->posv, m, 0, 64, s);
-    pgd_tmp_free(ctx, tmp);
+    const int eb = bits_for(m), end_bit = eb + bits_for(G.n + 2);
+    PGD_LAUNCH(ctx, k_plan_keys, grid_for(m), kThreads, 0, G, keys, vals, ctr, eb);
     unsigned long long cnt[4] = {0, 0, 0, 0};
     PGD_CUDA(ctx, cudaMemcpyAsync(cnt, ctr, sizeof(cnt), cudaMemcpyDeviceToHost, s));
     PGD_CUDA(ctx, cudaStreamSynchronize(s));
     P->nh = cnt[0];
     P->nd = cnt[3];
     P->nlight = m - (int64_t)P->nh - (int64_t)P->nd;
+    size_t tb = 0;
+    void *tmp = nullptr;
+    if (P->nd == (unsigned long long)m) {
+        // every position is a dense-graph edge: the sorted order is the identity
+        PGD_CUDA(ctx, cudaMemcpyAsync(P->posv, vals, m * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    } else {
+        cub::DeviceRadixSort::SortPairs(nullptr, tb, keys, keys2, vals, P->posv, m, 0, end_bit, s);
+        if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
+        cub::DeviceRadixSort::SortPairs(tmp, tb, keys, keys2, vals, P->posv, m, 0, end_bit, s);
+        pgd_tmp_free(ctx, tmp);
+    }
     const unsigned long long nh = P->nh;
     if (nh > 0) {
         if ((st = tg.alloc(&flag, (nh + 1) * sizeof(uint32_t)))) return st;
         if ((st = tg.alloc(&fpos, (nh + 1) * sizeof(uint32_t)))) return st;
-        PGD_LAUNCH(ctx, k_item_flags, grid_for(nh), kThreads, 0, keys2, (int64_t)nh, flag);
+        PGD_LAUNCH(ctx, k_item_flags, grid_for(nh), kThreads, 0, keys2, (int64_t)nh, flag, eb);
         PGD_CUDA(ctx, cudaMemsetAsync(flag + nh, 0, sizeof(uint32_t), s));
         tb = 0;
         cub::DeviceScan::ExclusiveSum(nullptr, tb, flag, fpos, (int64_t)nh + 1, s);
@@ -2713,13 +2729,14 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
     if (nd > 0 && dense) {
         // dense edges grouped by q, so that k_dense serves several per row pass
         // (edges of graphs with a CN matrix first, counted in ctr[7])
+        const int qb = bits_for(G.n), ebd = bits_for(G.npos);
         PGD_LAUNCH(ctx, k_dense_keys, grid_for(nd), kThreads, 0, G, posv + nh, (int64_t)nd,
-                   dense->cn ? dense->cbase : nullptr, keys, vals, ctr + 7);
+                   dense->cn ? dense->cbase : nullptr, keys, vals, ctr + 7, qb, ebd);
         size_t tbd = 0;
         void *tmpd = nullptr;
-        cub::DeviceRadixSort::SortPairs(nullptr, tbd, keys, keys2, vals, posv + nh, (int64_t)nd, 0, 64, s);
+        cub::DeviceRadixSort::SortPairs(nullptr, tbd, keys, keys2, vals, posv + nh, (int64_t)nd, 0, 1 + qb + ebd, s);
         if ((st = pgd_tmp_alloc(ctx, &tmpd, tbd))) return st;
-        cub::DeviceRadixSort::SortPairs(tmpd, tbd, keys, keys2, vals, posv + nh, (int64_t)nd, 0, 64, s);
+        cub::DeviceRadixSort::SortPairs(tmpd, tbd, keys, keys2, vals, posv + nh, (int64_t)nd, 0, 1 + qb + ebd, s);
         pgd_tmp_free(ctx, tmpd);
         int64_t ncn = 0;
         if (dense->cn) {
@@ -2730,7 +2747,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
         }
         TcOut tc;
         if (ncn > 0 && ctx->tc_min_deg > 0) {
-            if ((st = dense_tc(ctx, G, tg, dense, posv + nh, keys2, ncn, &tc))) return st;
+            if ((st = dense_tc(ctx, G, tg, dense, posv + nh, keys2, ncn, ebd, &tc))) return st;
             tc_ran = true;
         }
         if (ncn > 0) {
@@ -3387,14 +3404,14 @@ extern "C" pgd_status pgd_decompose_csr_noalloc(const int64_t *d_off, const int3
     G.top_r = 0;
     G.anchor_hub = kAnchorHub;
     k_tslot<<<grid_for(32 * m), kThreads, 0, s>>>(G, slot, nullptr, 0);
-    k_plan_keys<<<grid_for(m), kThreads, 0, s>>>(G, keys, vals, ctr);
+    k_plan_keys<<<grid_for(m), kThreads, 0, s>>>(G, keys, vals, ctr, 32);
     NA_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tb, keys, keys2, vals, posv, m, 0, 64, s));
     unsigned long long nh = 0;
     NA_CUDA(cudaMemcpyAsync(&nh, ctr, sizeof(nh), cudaMemcpyDeviceToHost, s));
     NA_CUDA(cudaStreamSynchronize(s));
     int64_t nitems = 0;
     if (nh > 0) {
-        k_item_flags<<<grid_for(nh), kThreads, 0, s>>>(keys2, (int64_t)nh, iflag);
+        k_item_flags<<<grid_for(nh), kThreads, 0, s>>>(keys2, (int64_t)nh, iflag, 32);
         NA_CUDA(cudaMemsetAsync(iflag + nh, 0, sizeof(uint32_t), s));
         NA_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, iflag, ipos, (int64_t)nh + 1, s));
         uint32_t ni = 0;
@@ -3553,8 +3570,8 @@ pgd_status pgd_dev_decompose_pairs_batch(pgd_ctx *ctx, int k, const int64_t *pai
     PB_TRY(pgd_tmp_alloc(ctx, (void **)&d_goff, (k + 1) * sizeof(int64_t)));
     PB_TRY(pgd_tmp_alloc(ctx, (void **)&gmax, (size_t)k * sizeof(int)));
     if (P > 0) {
-        PB_CUDA(cudaMemcpyAsync(d_src, src, P * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-        PB_CUDA(cudaMemcpyAsync(d_dst, dst, P * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        PB_CUDA(pgd_h2d(ctx, d_src, src, P * sizeof(int32_t)));
+        PB_CUDA(pgd_h2d(ctx, d_dst, dst, P * sizeof(int32_t)));
     }
     PB_CUDA(cudaMemcpyAsync(d_poff, pair_off, (k + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
     PB_CUDA(cudaMemsetAsync(gmax, 0xff, (size_t)k * sizeof(int), s));

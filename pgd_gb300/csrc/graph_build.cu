@@ -378,6 +378,28 @@ static pgd_status finish_csr(pgd_graph *g, uint64_t *keys, uint32_t *vals, int64
     return PGD_OK;
 }
 
+// 16-byte words from a mapped host source, then the tail bytes
+__global__ void k_copy_mapped(const uint4 *src, uint4 *dst, int64_t n16, const uint8_t *src_tail, uint8_t *dst_tail,
+                              int tail) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n16; i += stride) dst[i] = src[i];
+    if (blockIdx.x == 0 && threadIdx.x < tail) dst_tail[threadIdx.x] = src_tail[threadIdx.x];
+}
+
+cudaError_t pgd_h2d(pgd_ctx *ctx, void *dst, const void *src, size_t bytes) {
+    if (!bytes) return cudaSuccess;
+    const void *v = pgd_device_view(src);
+    if (!v || ((uintptr_t)v & 15) || ((uintptr_t)dst & 15))
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    const int64_t n16 = (int64_t)(bytes / 16);
+    const int tail = (int)(bytes % 16);
+    k_copy_mapped<<<ctx->num_sms * 8, kThreads, 0, ctx->stream>>>((const uint4 *)v, (uint4 *)dst, n16,
+                                                                   (const uint8_t *)v + 16 * n16,
+                                                                   (uint8_t *)dst + 16 * n16, tail);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
 pgd_status pgd_build_from_pairs(pgd_graph *g, const int32_t *h_src, const int32_t *h_dst, int64_t k, int64_t n_min,
                                 bool dedup) {
     pgd_ctx *ctx = g->ctx;
@@ -389,8 +411,8 @@ pgd_status pgd_build_from_pairs(pgd_graph *g, const int32_t *h_src, const int32_
     if ((st = pgd_tmp_alloc(ctx, (void **)&d_src, k1 * sizeof(int32_t)))) return st;
     if ((st = pgd_tmp_alloc(ctx, (void **)&d_dst, k1 * sizeof(int32_t)))) return st;
     if (k > 0) {
-        PGD_CUDA(ctx, cudaMemcpyAsync(d_src, h_src, k * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-        PGD_CUDA(ctx, cudaMemcpyAsync(d_dst, h_dst, k * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        PGD_CUDA(ctx, pgd_h2d(ctx, d_src, h_src, k * sizeof(int32_t)));
+        PGD_CUDA(ctx, pgd_h2d(ctx, d_dst, h_dst, k * sizeof(int32_t)));
     }
     st = pgd_build_from_device_pairs(g, d_src, d_dst, k, n_min, dedup);
     pgd_tmp_free(ctx, d_src);
@@ -860,6 +882,32 @@ __global__ void k_micro_ids(const int32_t *ev, const int32_t *eu, const int32_t 
         if (src1) src1[e] = (int64_t)ev[id] + 1;
         if (dst1) dst1[e] = (int64_t)eu[id] + 1;
     }
+}
+
+// The per-edge rows and their ids written straight into host memory that the
+// device can address (page-locked and mapped): one pass of every SM over the
+// host link, 16-byte stores.  Any of the three outputs may be null.
+__global__ void k_micro_out(const uint4 *micro, const int32_t *ev, const int32_t *eu, const int32_t *order,
+                            int64_t m, uint4 *cols, int64_t *src1, int64_t *dst1) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (cols)   // a row is 8 x 8 bytes = 4 x 16 bytes
+        for (int64_t i = t0; i < m * (PGD_NMICRO / 2); i += stride) cols[i] = micro[i];
+    if (src1 || dst1)
+        for (int64_t e = t0; e < m; e += stride) {
+            const int32_t id = order[e];
+            if (src1) src1[e] = (int64_t)ev[id] + 1;
+            if (dst1) dst1[e] = (int64_t)eu[id] + 1;
+        }
+}
+
+pgd_status pgd_dev_micro_out(pgd_graph *g, uint64_t *cols, int64_t *src1, int64_t *dst1) {
+    pgd_ctx *ctx = g->ctx;
+    if (g->norder > 0)
+        PGD_LAUNCH(ctx, k_micro_out, ctx->num_sms * 8, kThreads, 0, (const uint4 *)g->micro, g->ev, g->eu, g->order,
+                   g->norder, (uint4 *)cols, src1, dst1);
+    PGD_CUDA(ctx, cudaGetLastError());
+    return PGD_OK;
 }
 
 pgd_status pgd_dev_micro_ids(pgd_graph *g, int64_t *d_src1, int64_t *d_dst1) {

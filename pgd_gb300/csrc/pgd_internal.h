@@ -121,6 +121,13 @@ pgd_status pgd_dev_cores(pgd_graph *g);
 pgd_status pgd_dev_assortativity(pgd_graph *g, double *r);
 pgd_status pgd_dev_sort_edges(pgd_graph *g, int order_kind, int s2l);
 pgd_status pgd_dev_sort_edges_sample(pgd_graph *g, int order_kind, int s2l, const int64_t *h_ids, int64_t k);
+pgd_status pgd_dev_micro_out(pgd_graph *g, uint64_t *cols, int64_t *src1, int64_t *dst1);
+// host memory the device can address directly (page-locked, mapped): its device address, else null
+void *pgd_device_view(const void *host);
+// host -> device copy on the context's stream: a kernel through the mapping when
+// the source is page-locked host memory (every SM's bandwidth over the host
+// link), else cudaMemcpyAsync
+cudaError_t pgd_h2d(pgd_ctx *ctx, void *dst, const void *src, size_t bytes);
 pgd_status pgd_dev_micro_ids(pgd_graph *g, int64_t *d_src1, int64_t *d_dst1);
 
 // Decomposition (decompose.cu).
