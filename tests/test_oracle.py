@@ -315,3 +315,44 @@ def test_c4_identity_used_by_the_kernels(seed):
             Sq[p] = False
             got = int(W[Sq, p].sum()) - int(Sq.sum()) - int(W[T, q].sum()) + 2 * k4 + t
             assert got == c4, (p, q, got, c4)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_dense_tensor_core_identities(seed):
+    """What the tensor-core kernels of dense batch graphs compute, restated in
+    integer numpy and checked against the oracle's per-edge k4 and c4:
+      2·k4(p, q) = sum_{y in N(q)} A_py · D[p][y], D = C_q C_q^T over the ego
+        network of q compacted to N(q)'s columns (k_dense_tc, for the edges
+        (p, q) of q's run);
+      c4 = E[q][p] - d_p + 2·k4 + t - |S_q|, E = A·(CN - A∘CN) - (A∘CN)·A,
+        CN = A², |S_q| = d_q - t - 1 (k_dense_gram + k_dense_close)."""
+    rng = np.random.default_rng(300 + seed)
+    n = int(rng.integers(30, 120))
+    p_edge = float(rng.uniform(0.1, 0.8))
+    iu, ju = np.triu_indices(n, 1)
+    keep = rng.random(len(iu)) < p_edge
+    src, dst = iu[keep].astype(np.int32), ju[keep].astype(np.int32)
+    og = ol.OracleGraph.from_pairs(src, dst, dedup=True)
+    og.run(order="kcore", micro=True)
+    s1, d1, cols = og.micro()
+    off, adj = og.csr()
+    nn = len(off) - 1
+    A = np.zeros((nn, nn), np.int64)
+    for v in range(nn):
+        A[v, adj[off[v]:off[v + 1]]] = 1
+    deg = A.sum(1)
+    CN = A @ A
+    TA = A * CN
+    E = A @ (CN - TA) - TA @ A
+    assert (E == E.T).all()
+    assert len(cols) == og.m > 0
+    for (a, b), row in zip(zip(s1 - 1, d1 - 1), cols):
+        t, k4, c4 = int(row[0]), int(row[2]), int(row[5])
+        for p, q in ((a, b), (b, a)):
+            nq = np.flatnonzero(A[q])
+            C = A[np.ix_(nq, nq)]          # ego network of q, compacted to N(q)'s columns
+            j = int(np.searchsorted(nq, p))
+            assert (C[j] @ (C @ C[j])) == 2 * k4
+            assert CN[p, q] == t
+            got = int(E[q, p]) - int(deg[p]) + 2 * k4 + t - (int(deg[q]) - t - 1)
+            assert got == c4, (p, q, got, c4)
