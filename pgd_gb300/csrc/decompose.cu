@@ -1568,6 +1568,23 @@ __global__ void k_tc_run_flags(const uint64_t *keys, int64_t ncn, const int32_t 
     }
 }
 
+// positions of the CN-graph edges whose q's degree is outside [min_deg,
+// kTcMaxDeg]: the ones k_dense_cn decomposes, kept in their order
+__global__ void k_tc_rest_flags(const uint64_t *keys, int64_t ncn, const int32_t *deg, int min_deg, uint32_t *flag,
+                                int eb) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ncn; i += (int64_t)gridDim.x * blockDim.x) {
+        const int d = deg[(uint32_t)(keys[i] >> eb)];
+        flag[i] = (d < min_deg || d > kTcMaxDeg) ? 1u : 0u;
+    }
+}
+
+__global__ void k_tc_rest_fill(const int32_t *dpos, const uint32_t *flag, const uint32_t *pos, int64_t ncn,
+                               int32_t *rest, unsigned long long *nrest) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ncn; i += (int64_t)gridDim.x * blockDim.x)
+        if (flag[i]) rest[pos[i]] = dpos[i];
+    if (blockIdx.x == 0 && threadIdx.x == 0) *nrest = pos[ncn];
+}
+
 __global__ void k_tc_run_fill(const uint64_t *keys, const uint32_t *flag, const uint32_t *pos, int64_t ncn,
                               int64_t *runs, unsigned long long *nruns, int eb) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ncn; i += (int64_t)gridDim.x * blockDim.x) {
@@ -2429,12 +2446,15 @@ struct DenseView {
 // (k_dense_gram).  out->k4 gets k4 per position of dpos (0xffffffff outside
 // those runs), out->eslot E per adjacency slot, out->runs the runs.  ctr[8..10]: run counter, run
 // count and failed-wait count; ctr[11]: the run counter of k_dense_close;
-// ctr[12]: the item counter of k_dense_gram.
+// ctr[12]: the item counter of k_dense_gram; ctr[13]: the count of positions
+// left to k_dense_cn (out->rest, out->nrest).
 struct TcOut {
     uint32_t *k4 = nullptr;
     int32_t *eslot = nullptr;
     int64_t *runs = nullptr;
     const unsigned long long *nruns = nullptr;
+    int32_t *rest = nullptr;    // positions left to k_dense_cn, in dpos order
+    int64_t nrest = 0;
 };
 
 static pgd_status dense_tc(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, const DenseView *dense,
@@ -2449,7 +2469,7 @@ static pgd_status dense_tc(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, const 
     if ((st = tg.alloc(&k4, ncn * sizeof(uint32_t)))) return st;
     if ((st = tg.alloc(&runs, (2 * maxruns + 2) * sizeof(int64_t)))) return st;
     unsigned long long *ctr = ctx->d_ctr;
-    PGD_CUDA(ctx, cudaMemsetAsync(ctr + 8, 0, 5 * sizeof(unsigned long long), s));
+    PGD_CUDA(ctx, cudaMemsetAsync(ctr + 8, 0, 6 * sizeof(unsigned long long), s));
     PGD_LAUNCH(ctx, k_tc_run_flags, grid_for(ncn), kThreads, 0, keys, ncn, G.deg, ctx->tc_min_deg, flag, eb);
     PGD_CUDA(ctx, cudaMemsetAsync(flag + ncn, 0, sizeof(uint32_t), s));
     size_t tb = 0;
@@ -2501,10 +2521,26 @@ static pgd_status dense_tc(pgd_ctx *ctx, const DevGraph &G, TmpGuard &tg, const 
     E.next = ctr + 12;
     E.err = ctr + 10;
     PGD_LAUNCH(ctx, k_dense_gram, ctx->num_sms, kGramThreads, kGramSmem, E);
+    // the positions left to k_dense_cn (flag and pos arrays reused)
+    int32_t *rest = nullptr;
+    if ((st = tg.alloc(&rest, (ncn + 1) * sizeof(int32_t)))) return st;
+    PGD_LAUNCH(ctx, k_tc_rest_flags, grid_for(ncn), kThreads, 0, keys, ncn, G.deg, ctx->tc_min_deg, flag, eb);
+    PGD_CUDA(ctx, cudaMemsetAsync(flag + ncn, 0, sizeof(uint32_t), s));
+    tb = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tb, flag, pos, ncn + 1, s);
+    if ((st = pgd_tmp_alloc(ctx, &tmp, tb))) return st;
+    cub::DeviceScan::ExclusiveSum(tmp, tb, flag, pos, ncn + 1, s);
+    pgd_tmp_free(ctx, tmp);
+    PGD_LAUNCH(ctx, k_tc_rest_fill, grid_for(ncn), kThreads, 0, dpos, flag, pos, ncn, rest, ctr + 13);
+    unsigned long long nrest = 0;
+    PGD_CUDA(ctx, cudaMemcpyAsync(&nrest, ctr + 13, sizeof(nrest), cudaMemcpyDeviceToHost, s));
+    PGD_CUDA(ctx, cudaStreamSynchronize(s));
     out->k4 = k4;
     out->eslot = eslot;
     out->runs = runs;
     out->nruns = ctr + 9;
+    out->rest = rest;
+    out->nrest = (int64_t)nrest;
     return PGD_OK;
 }
 
@@ -2750,7 +2786,7 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
             if ((st = dense_tc(ctx, G, tg, dense, posv + nh, keys2, ncn, ebd, &tc))) return st;
             tc_ran = true;
         }
-        if (ncn > 0) {
+        if (ncn > 0 && (!tc.k4 || tc.nrest > 0)) {
             DenseCnArgs C;
             C.G = G;
             C.bits = dense->bits;
@@ -2758,11 +2794,14 @@ static pgd_status run_decompose(pgd_ctx *ctx, const DevGraph &G, int4 *slot, int
             C.vbase = dense->vbase;
             C.cn = dense->cn;
             C.cbase = dense->cbase;
-            C.dpos = posv + nh;
-            C.k4pre = tc.k4;
-            C.ndense = ncn;
+            // with the tensor-core path, only the positions outside its runs
+            C.dpos = tc.k4 ? tc.rest : posv + nh;
+            C.k4pre = nullptr;
+            C.ndense = tc.k4 ? tc.nrest : ncn;
             C.next = ctr + 6;
             PGD_LAUNCH(ctx, k_dense_cn, nsm * 8, 256, 0, C);
+        }
+        if (ncn > 0) {
             if (tc.k4) {
                 DenseCloseArgs Z;
                 Z.G = G;
