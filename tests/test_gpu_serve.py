@@ -124,3 +124,32 @@ def test_server_admits_small_requests_past_a_large_one():
     assert s["queue_p50_ms"] <= s["queue_p99_ms"] and s["service_p50_ms"] <= s["service_p99_ms"]
     assert s["p99_ms"] >= s["p50_ms"] > 0
     sv.close()
+
+
+def test_server_dense_requests_on_both_workers():
+    """Dense requests take the tensor-core kernels inside the server's batches,
+    on both workers' streams at once: every result equals the single-graph
+    kernels' (which never use the tensor cores) and, for the smaller graphs,
+    the oracle's."""
+    rng = np.random.default_rng(11)
+    graphs = []
+    for i in range(24):
+        n = int(rng.integers(150, 900)) if i % 3 else int(rng.integers(40, 120))
+        graphs.append(pgd.erdos_renyi(n, float(rng.uniform(0.3, 0.8)), seed=700 + i))
+    ctx = pgd.Context()
+    want = []
+    for s, d in graphs:
+        g = ctx.graph_from_edges(s, d)
+        want.append(g.decompose(micro=False).totals)
+        g.destroy()
+    ctx.close()
+    sv = pgd.Server(workers=2)
+    tickets = [sv.submit(s, d) for s, d in graphs]
+    for i, tk in enumerate(tickets):
+        st, r = sv.wait(tk, 120000)
+        assert st == 0
+        assert (r.totals == want[i]).all(), i
+        if i % 3 == 0:
+            assert (r.totals == oracle_totals(*graphs[i])).all(), i
+    assert sv.stats()["completed"] == len(graphs)
+    sv.close()
