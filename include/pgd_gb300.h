@@ -275,7 +275,10 @@ pgd_status pgd_server_destroy(pgd_server *sv);
 
 /* ---- thresholds and autotuning (no reference counterpart) --------------
  * Three thresholds steer how the decomposition kernels split work; counts
- * never depend on them.  anchor_hub (2..256, default 64): anchors of degree
+ * never depend on them.  Until the caller sets them (here or through
+ * pgd_autotune), graphs of more than 8·2^20 vertices are decomposed with
+ * anchor_hub 128 and cache_hub 40, the faster pair on large power-law
+ * graphs.  anchor_hub (2..256, default 64): anchors of degree
  * >= it are processed one CTA per anchor with N(p) as a bitmap, below it one
  * warp per edge with N(p) staged and searched.  cache_hub (>= 2, default
  * 32): W(w,p) comes from the anchor's histogram for neighbours of degree >=

@@ -28,6 +28,7 @@ struct pgd_ctx {
     int cache_hub = 32;      // W(w,p) taken from the per-anchor histogram for neighbours of degree >= this
     int dense_max = 2048;    // batched graphs with at most this many vertices use row bitsets
     int tc_min_deg = 64;     // batched CN-graph runs with d_q >= this count k4 on the tensor cores (0: never)
+    bool thresholds_set = false;   // anchor_hub / cache_hub chosen by the caller or pgd_autotune
 };
 
 struct pgd_graph {

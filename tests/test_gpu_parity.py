@@ -268,3 +268,38 @@ def test_repeat_decompositions_are_identical(ctx):
     b = g.decompose(micro=True)
     cb = g.micro(ids=False)
     assert (a.totals == b.totals).all() and (ca == cb).all()
+
+
+def test_large_graph_default_thresholds():
+    """Graphs of more than 8·2^20 vertices take hub thresholds 128 / 40 while
+    the caller has set none; counts must not change (against the oracle and
+    against the 64 / 32 thresholds set explicitly), and the context's
+    thresholds stay as they were."""
+    s, d = pgd.rmat(14, 8, seed=6)
+    n = (8 << 20) + 1000
+    c = pgd.Context()
+    before = c.thresholds()
+    g = c.graph_from_edges(s, d, n_min=n)
+    assert g.n == n
+    g.preprocess("deg")
+    g.compute_cores()
+    g.sort_edges("kcore")
+    r = g.decompose(micro=True)
+    assert c.thresholds() == before
+    rows = g.micro()
+    c2 = pgd.Context()
+    c2.set_thresholds(64, 32, 2048)
+    g2 = c2.graph_from_edges(s, d, n_min=n)
+    g2.preprocess("deg")
+    g2.compute_cores()
+    g2.sort_edges("kcore")
+    r2 = g2.decompose(micro=True)
+    assert (r.totals == r2.totals).all() and (r.sums == r2.sums).all()
+    for a, b in zip(rows, g2.micro()):
+        assert (a == b).all()
+    o = ol.OracleGraph.from_pairs(s, d, n_min=n, dedup=True).run(order="kcore", micro=False)
+    assert (r.totals == o.totals()).all()
+    g.destroy()
+    g2.destroy()
+    c.close()
+    c2.close()
