@@ -276,7 +276,7 @@ pgd_status pgd_server_destroy(pgd_server *sv);
 /* ---- thresholds and autotuning (no reference counterpart) --------------
  * Three thresholds steer how the decomposition kernels split work; counts
  * never depend on them.  Until the caller sets them (here or through
- * pgd_autotune), graphs of more than 8·2^20 vertices are decomposed with
+ * pgd_autotune), graphs of more than 1.5·2^20 vertices are decomposed with
  * anchor_hub 128 and cache_hub 40, the faster pair on large power-law
  * graphs.  anchor_hub (2..256, default 64): anchors of degree
  * >= it are processed one CTA per anchor with N(p) as a bitmap, below it one

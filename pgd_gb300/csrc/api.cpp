@@ -365,10 +365,11 @@ extern "C" pgd_status pgd_decompose(pgd_graph *g, uint32_t flags, pgd_counts *ou
     // Default thresholds by graph size (counts never depend on them): while the
     // caller has set none (directly or through pgd_autotune), graphs of more
     // than kLargeGraph vertices take hub anchors from degree 128 and cached W
-    // from degree 40.  Measured on RMAT scale 24: 53.3 s against 56.5 s with
-    // the 64 / 32 defaults, which stay the fastest on RMAT scale 20.
+    // from degree 40.  Measured on RMAT scales 21 to 24 (2.1 M to 16.8 M
+    // vertices): 0.3 %, 1.2 %, 1.0 % and 5.7 % faster than the 64 / 32
+    // defaults, which stay the fastest on RMAT scale 20 (1.05 M vertices).
     pgd_ctx *ctx = g->ctx;
-    constexpr int64_t kLargeGraph = 8ll << 20;
+    constexpr int64_t kLargeGraph = 3ll << 19;   // 1.5 * 2^20
     if (!ctx->thresholds_set && g->n > kLargeGraph) {
         const int a = ctx->anchor_hub, c = ctx->cache_hub;
         ctx->anchor_hub = 128;

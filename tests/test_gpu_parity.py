@@ -271,7 +271,7 @@ def test_repeat_decompositions_are_identical(ctx):
 
 
 def test_large_graph_default_thresholds():
-    """Graphs of more than 8·2^20 vertices take hub thresholds 128 / 40 while
+    """Graphs of more than 1.5·2^20 vertices take hub thresholds 128 / 40 while
     the caller has set none; counts must not change (against the oracle and
     against the 64 / 32 thresholds set explicitly), and the context's
     thresholds stay as they were."""
