@@ -96,3 +96,21 @@ def test_generators_are_deterministic_and_shaped():
     assert len(s) == 10 + (500 - 5) * 4
     s, d = pgd.rgg3d(2000, 0.1, seed=5)
     assert len(s) > 0 and (s < d).all()
+
+
+def test_concat_pairs_layout():
+    """The flat batch format of pgd_decompose_pairs_batch: graph i's pairs are
+    src/dst[off[i]:off[i + 1]], int32 ids, int64 offsets (no device needed)."""
+    import numpy as np
+
+    import pgd_gb300 as pgd
+
+    graphs = [(np.array([0, 1, 2], np.int64), np.array([1, 2, 0], np.int64)),
+              (np.zeros(0, np.int32), np.zeros(0, np.int32)),
+              (np.array([5], np.int32), np.array([7], np.int32))]
+    off, src, dst = pgd.concat_pairs(graphs)
+    assert off.dtype == np.int64 and src.dtype == np.int32 and dst.dtype == np.int32
+    assert off.tolist() == [0, 3, 3, 4]
+    assert src.tolist() == [0, 1, 2, 5] and dst.tolist() == [1, 2, 0, 7]
+    off0, src0, dst0 = pgd.concat_pairs([])
+    assert off0.tolist() == [0] and len(src0) == 0 and len(dst0) == 0
