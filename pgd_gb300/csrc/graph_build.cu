@@ -403,18 +403,22 @@ cudaError_t pgd_h2d(pgd_ctx *ctx, void *dst, const void *src, size_t bytes) {
 pgd_status pgd_build_from_pairs(pgd_graph *g, const int32_t *h_src, const int32_t *h_dst, int64_t k, int64_t n_min,
                                 bool dedup) {
     pgd_ctx *ctx = g->ctx;
-    cudaStream_t s = ctx->stream;
     if (k < 0 || k > (int64_t)0x7fffffff) return pgd_fail(ctx, PGD_EINVAL, "pair count out of range (0..2^31-1)");
     pgd_status st;
     int32_t *d_src = nullptr, *d_dst = nullptr;
     const int64_t k1 = k > 0 ? k : 1;
     if ((st = pgd_tmp_alloc(ctx, (void **)&d_src, k1 * sizeof(int32_t)))) return st;
-    if ((st = pgd_tmp_alloc(ctx, (void **)&d_dst, k1 * sizeof(int32_t)))) return st;
-    if (k > 0) {
-        PGD_CUDA(ctx, pgd_h2d(ctx, d_src, h_src, k * sizeof(int32_t)));
-        PGD_CUDA(ctx, pgd_h2d(ctx, d_dst, h_dst, k * sizeof(int32_t)));
+    if ((st = pgd_tmp_alloc(ctx, (void **)&d_dst, k1 * sizeof(int32_t)))) {
+        pgd_tmp_free(ctx, d_src);
+        return st;
     }
-    st = pgd_build_from_device_pairs(g, d_src, d_dst, k, n_min, dedup);
+    cudaError_t e = cudaSuccess;
+    if (k > 0) {
+        e = pgd_h2d(ctx, d_src, h_src, k * sizeof(int32_t));
+        if (e == cudaSuccess) e = pgd_h2d(ctx, d_dst, h_dst, k * sizeof(int32_t));
+    }
+    st = e == cudaSuccess ? pgd_build_from_device_pairs(g, d_src, d_dst, k, n_min, dedup)
+                          : pgd_cuda_fail(ctx, e, "upload of the pairs");
     pgd_tmp_free(ctx, d_src);
     pgd_tmp_free(ctx, d_dst);
     return st;
